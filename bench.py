@@ -1,0 +1,380 @@
+"""Benchmark: 30-qubit f64 random circuit (depth 40 + qft) on one GB300, qvnt semantics.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one run of the workload circuit on a resident 30-qubit register: reset to |0> and
+apply the 2,985-gate queue (40 layers of {h, s, t, u3} on every qubit, 15 random two-qubit gates
+from {rxx, ryy, rzz, swap, i_swap, sqrt_i_swap}, 3 Toffolis, then qft over all 30 qubits).
+Inputs are seeded synthetic circuits (no public suite).  The state (16 GiB) is larger than L2
+(129 MB), so no flush is needed between steps.
+
+Printed as one JSON line (rank 0):
+  value        unfused gate passes per second (qvnt SingleOps), whole job, device-timed
+  e2e          the same metric through the plugin call qvnt_apply_host (Applicable::apply): the
+               state goes host -> device -> host from pinned memory inside the timed region
+  roofline     the fused-pass kernel: algorithmic bytes (2 x 2^30 x 16 B per pass) / its average
+               CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline the CPU oracle (qvnt's algorithm restated in C, OpenMP on every host core) on a
+               bounded sample of the same circuit at 30 qubits
+--impl reference times only that CPU implementation (the reference is Rust; no cargo exists here).
+With N > 1 (torchrun) each rank runs an independent replica on its own GPU ("replicas only").
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = 30
+DEPTH = 40
+SEED = 2
+AMP_BYTES = 16
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "fused_pass_traffic.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--qubits", type=int, default=N_QUBITS)
+    ap.add_argument("--depth", type=int, default=DEPTH)
+    ap.add_argument("--engine", default="fused", choices=["fused", "plain"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=1, help="steps of the plain f64 GPU path (0 = skip)")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, ws, rank, local, backend):
+        self.ws, self.rank = ws, rank
+        self.pg = None
+        if ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group(backend=backend, rank=rank, world_size=ws)
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device="cuda" if self.td.get_backend() == "nccl" else "cpu")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device="cuda" if self.td.get_backend() == "nccl" else "cpu")
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_pass_bytes(n):
+    return 2 * (1 << n) * AMP_BYTES
+
+
+def cpu_sample(circ_gates, n, budget_s=12.0):
+    """The oracle (qvnt's algorithm: one out-of-place gather pass per gate, OpenMP over amplitudes)
+    on the first gates of the same circuit at the same register size; returns (gates/s, threads,
+    gates timed)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import oracle_ref as orc
+    threads = orc.max_threads()
+    psi = orc.new_state(n, 0)
+    scratch = np.empty_like(psi)
+    arr = orc.arr(circ_gates)
+    lib = orc.lib()
+    done, t_total = 0, 0.0
+    # one gate at a time, until the budget is spent
+    while done < len(circ_gates) and t_total < budget_s:
+        t0 = time.perf_counter()
+        lib.oracle_apply(ctypes.byref(arr[done]), 1, psi.ctypes.data, scratch.ctypes.data, psi.size, threads)
+        t_total += time.perf_counter() - t0
+        done += 1
+    return done / t_total, threads, done
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: qvnt's CPU algorithm on the host cores (the C restatement; the Rust crate
+    cannot be built here), rank 0 only."""
+    if rank != 0:
+        return
+    from qvnt_gb300.circuits import random_circuit
+    circ = random_circuit(args.qubits, args.depth, seed=SEED)
+    gates = circ.gates()
+    vals = []
+    threads = 1
+    for i in range(args.warmup + args.steps):
+        v, threads, done = cpu_sample(gates, args.qubits, budget_s=8.0)
+        if i >= args.warmup:
+            vals.append(v)
+    value = sum(vals) / len(vals)
+    unit = "gate-passes/s"
+    line = {
+        "impl": "reference", "metric": "%dq gate-passes/s" % args.qubits, "value": value, "unit": unit,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64 circuit)",
+        "config": {"workload": "random circuit %dq depth %d + qft, %d gates" % (args.qubits, args.depth, len(gates)),
+                   "n_qubits": args.qubits, "depth": args.depth, "gates": len(gates)},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port",
+                         "sample": "first gates of the circuit, ~8 s per step, at %d qubits" % args.qubits},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import numpy as np
+    import torch
+    from qvnt_gb300 import ENGINE_FUSED, ENGINE_PLAIN, Context, QReg
+    from qvnt_gb300._abi import gate_array
+    from qvnt_gb300.circuits import random_circuit
+
+    torch.cuda.set_device(local)
+    dist = Dist(ws, rank, local, "nccl")
+    ctx = Context(local)
+    n = args.qubits
+    circ = random_circuit(n, args.depth, seed=SEED)
+    gates = circ.gates()
+    garr = gate_array(gates)
+    ngates = len(gates)
+    engine = ENGINE_FUSED if args.engine == "fused" else ENGINE_PLAIN
+
+    q = QReg(n, 0, ctx=ctx)
+    q.set_engine(engine)
+    stream = torch.cuda.ExternalStream(q.stream())
+
+    def step():
+        q.reset(0)
+        q.apply_gates(garr, ngates)
+
+    for _ in range(args.warmup):
+        step()
+    q.sync()
+    launches0, passes0 = q.stats()
+    q.kernel_timing(enable=1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_time(ev1)
+    kern_ms, kern_n = q.kernel_timing(enable=0)
+    launches1, passes1 = q.stats()
+    ms_max = dist.max(dev_ms)
+    gpu_launches = int(dist.sum(launches1 - launches0))
+    passes_per_step = (passes1 - passes0) / args.steps
+
+    units = ngates * args.steps * ws
+    value = units / (ms_max / 1e3)
+    pass_bytes = algorithmic_pass_bytes(n)
+    hbm_gbs = passes_per_step * args.steps * pass_bytes / (dev_ms / 1e3) / 1e9
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    if not peak:
+        peak = 6800.0
+    avg_launch_ms = kern_ms / kern_n if kern_n else None
+    achieved = pass_bytes / (avg_launch_ms / 1e3) / 1e9 if avg_launch_ms else None
+    traffic = None
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            tr = json.load(f)
+        traffic = tr.get("bytes_per_full_launch_%dq" % n)
+    except Exception:
+        pass
+
+    # plain f64 GPU path on the same workload (one pass per SingleOp), for the comparison the metric names
+    plain = None
+    if args.plain_steps > 0 and engine == ENGINE_FUSED:
+        qp = QReg(n, 0, ctx=ctx)
+        qp.set_engine(ENGINE_PLAIN)
+        sp = torch.cuda.ExternalStream(qp.stream())
+        qp.reset(0)
+        qp.apply_gates(garr, ngates)  # warm-up
+        qp.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(sp)
+        for _ in range(args.plain_steps):
+            qp.reset(0)
+            qp.apply_gates(garr, ngates)
+        e1.record(sp)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1)
+        plain = {"value": ngates * args.plain_steps / (pms / 1e3), "unit": "gate-passes/s",
+                 "ms_per_step": pms / args.plain_steps, "steps": args.plain_steps}
+        qp.close()
+        del qp
+
+    # e2e through the plugin call with host buffers (Applicable::apply semantics)
+    e2e = None
+    if not args.no_e2e:
+        q.close()
+        del q
+        torch.cuda.synchronize()
+        length = max(1 << n, 8)
+        hin = torch.zeros(length * 2, dtype=torch.float64, pin_memory=True)
+        hout = torch.empty(length * 2, dtype=torch.float64, pin_memory=True)
+        hin[0] = 1.0
+        nin = hin.numpy().view(np.complex128)
+        nout = hout.numpy().view(np.complex128)
+
+        def e2e_step():
+            ctx.apply_host(circ, nin, nout)
+
+        e2e_step()  # warm-up (allocates the context's plugin register)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        dist.barrier()
+        e2e_s = dist.max(time.perf_counter() - t0)
+        e2e = {"value": ngates * args.steps * ws / e2e_s, "unit": "gate-passes/s",
+               "h2d_bytes_per_step": length * AMP_BYTES + ngates * ctypes.sizeof(gates[0]),
+               "d2h_bytes_per_step": length * AMP_BYTES}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, threads, done = cpu_sample(gates, n)
+        cpu = {"value": v, "unit": "gate-passes/s", "cores": threads, "kind": "port",
+               "sample": "first %d gates of the circuit at %d qubits (oracle, OpenMP)" % (done, n)}
+
+    if rank == 0:
+        line = {
+            "metric": "%dq gate-passes/s" % n,
+            "value": value,
+            "unit": "gate-passes/s",
+            "n_gpus": ws,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded SplitMix64 random circuit)",
+            "config": {"workload": "random circuit %dq f64, depth %d + qft, %d gates" % (n, args.depth, ngates),
+                       "n_qubits": n, "depth": args.depth, "gates": ngates, "engine": args.engine,
+                       "fused_passes_per_step": passes_per_step,
+                       "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "state %d GiB > L2 129 MB, no flush" % ((1 << n) * AMP_BYTES >> 30)},
+            "hbm_gbs": hbm_gbs,
+            "circuits_per_s": ws * args.steps / (ms_max / 1e3),
+            "wall_s": wall,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "peak_source": peak_src, "kernel": "fused_pass_kernel" if engine == ENGINE_FUSED else "plain_gate_kernel",
+                         "launches_timed": kern_n, "avg_launch_ms": avg_launch_ms},
+            "plain_f64_gpu": plain,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": gpu_launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,243 @@
+/*
+ * qvnt_gb300.h - C ABI of the GB300 state-vector engine for qvnt.
+ *
+ * The engine replaces the state-owning half of qvnt's `QReg` and the per-amplitude
+ * gate loops under it (qvnt 0.4.4):
+ *   - `trait Applicable { apply; apply_sync; act_on; dgr; c }`  src/operator/applicable.rs:5-15
+ *   - `QReg::{new, with_state, apply, measure_mask, get_probabilities, get_absolute, get_polar}`
+ *                                                                src/register/quant.rs:113-505
+ *   - `AtomicOp::for_each{,_par}` over the 20 atomic gates      src/operator/atomic/dispatch.rs:28-105
+ *
+ * A host that keeps qvnt's own circuit building (Rust `op::`, `MultiOp`, `SingleOp`) lowers each
+ * `SingleOp{act, ctrl, func}` (src/operator/single/mod.rs:42-47) to one `qvnt_gate` and hands the
+ * queue to `qvnt_reg_apply`.  The state vector lives only in GPU memory; there is no CPU path.
+ *
+ * Conventions
+ *   - Every function returns a status code (`QVNT_OK` = 0).  No exception or abort crosses the ABI.
+ *     `qvnt_last_error()` returns a thread-local message for the last failing call on this thread.
+ *   - Amplitude index i is the basis state |i>, qubit q is bit q of i (LSB = qubit 0).
+ *   - Host amplitude buffers are interleaved (re, im) doubles, `Complex<f64>` layout.
+ *   - A register holds `max(2^n, 8)` amplitudes, as `QReg` does (src/register/quant.rs:15, :113-150).
+ *   - One register maps to one CUDA stream.  A register handle is not thread-safe; different
+ *     registers may be used from different threads.
+ */
+#ifndef QVNT_GB300_H
+#define QVNT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------------------
+ * Status codes.  qvnt panics (`expect`, index out of bounds) or returns `None` where these are
+ * returned instead (src/operator/mod.rs:151-155, src/operator/single/mod.rs:4-11, :108-118).
+ * ------------------------------------------------------------------------------------------- */
+enum qvnt_status {
+    QVNT_OK = 0,
+    QVNT_ERR_OOM = 1,         /* device allocation failed                                    */
+    QVNT_ERR_BAD_MASK = 2,    /* mask outside the register, wrong bit count, ctrl overlaps act */
+    QVNT_ERR_BAD_HANDLE = 3,  /* null or destroyed handle                                    */
+    QVNT_ERR_CUDA = 4,        /* CUDA runtime error (message in qvnt_last_error)             */
+    QVNT_ERR_TIMEOUT = 5,     /* a bounded device wait ran out                               */
+    QVNT_ERR_BAD_ARG = 6,     /* other invalid argument (null pointer, bad kind, size)       */
+    QVNT_ERR_UNSUPPORTED = 7  /* operation not supported by the engine                       */
+};
+
+/* ---------------------------------------------------------------------------------------------
+ * Gate kinds, numbered in the order of `enum AtomicOpDispatch` (src/operator/atomic/dispatch.rs:82-105).
+ * ------------------------------------------------------------------------------------------- */
+enum qvnt_gate_kind {
+    QVNT_GATE_ID = 0,          /* atomic/id.rs                                        */
+    QVNT_GATE_X = 1,           /* atomic/x.rs    any mask, one pass                   */
+    QVNT_GATE_RX = 2,          /* atomic/rx.rs   1-bit mask                           */
+    QVNT_GATE_RXX = 3,         /* atomic/rxx.rs  2-bit mask                           */
+    QVNT_GATE_Y = 4,           /* atomic/y.rs    any mask                             */
+    QVNT_GATE_RY = 5,          /* atomic/ry.rs   1-bit mask                           */
+    QVNT_GATE_RYY = 6,         /* atomic/ryy.rs  2-bit mask                           */
+    QVNT_GATE_Z = 7,           /* atomic/z.rs    any mask                             */
+    QVNT_GATE_S = 8,           /* atomic/s.rs    any mask, dagger flag                */
+    QVNT_GATE_T = 9,           /* atomic/t.rs    any mask, dagger flag                */
+    QVNT_GATE_RZ = 10,         /* atomic/rz.rs   1-bit mask                           */
+    QVNT_GATE_RZZ = 11,        /* atomic/rzz.rs  2-bit mask                           */
+    QVNT_GATE_U1 = 12,         /* atomic/u1.rs   1-bit mask, dense 2x2                */
+    QVNT_GATE_U2 = 13,         /* atomic/u2.rs   a_mask + b_mask, dense 4x4           */
+    QVNT_GATE_H1 = 14,         /* atomic/h1.rs   1-bit mask                           */
+    QVNT_GATE_H2 = 15,         /* atomic/h2.rs   a_mask + b_mask (1 bit each)         */
+    QVNT_GATE_SWAP = 16,       /* atomic/swap.rs 2-bit mask                           */
+    QVNT_GATE_ISWAP = 17,      /* atomic/i_swap.rs 2-bit mask, dagger flag            */
+    QVNT_GATE_SQRT_SWAP = 18,  /* atomic/sqrt_swap.rs 2-bit mask, dagger flag         */
+    QVNT_GATE_SQRT_ISWAP = 19, /* atomic/sqrt_i_swap.rs 2-bit mask, dagger flag       */
+    QVNT_GATE_KIND_COUNT = 20
+};
+
+/* One lowered `SingleOp` (src/operator/single/mod.rs:42-47): the atomic function plus its control
+ * mask.  Fields a gate kind does not use must be zero.
+ *   a_mask  X/Y/Z/S/T/RX/RY/RZ/H1/U1: the `a_mask`;  RXX/RYY/RZZ/SWAP/ISWAP/SQRT_*: the `ab_mask`;
+ *           H2/U2: the `a_mask` (one bit).
+ *   b_mask  H2/U2 only: the `b_mask` (one bit).
+ *   ctrl    `SingleOp::ctrl`: the gate acts where all ctrl bits are 1 (dispatch.rs:35).
+ *   dagger  S/T/ISWAP/SQRT_SWAP/SQRT_ISWAP: the `dagger` field of the atomic op.
+ *   phase   RX/RY/RZ/RXX/RYY/RZZ: the STORED phase (cos(theta/2), sin(theta/2)) after any `.dgr()`,
+ *           which negates both parts (rx.rs:10-14, :42-47).  Carrying the stored phase keeps qvnt's
+ *           `.dgr()` semantics, -R(theta), exactly.
+ *   matrix  U1: 2x2, U2: 4x4 complex matrix, row-major, interleaved (re, im) (u1.rs:17-25, u2.rs:22-49).
+ */
+typedef struct qvnt_gate {
+    uint32_t kind;
+    uint32_t dagger;
+    uint64_t a_mask;
+    uint64_t b_mask;
+    uint64_t ctrl;
+    double phase[2];
+    double matrix[32];
+} qvnt_gate;
+
+typedef struct qvnt_ctx qvnt_ctx;
+typedef struct qvnt_reg qvnt_reg;
+
+/* Engines a register can run its gate queue on.
+ *   FUSED  (default) groups runs of gates into fused passes staged through shared memory.
+ *   PLAIN  runs one in-place FP64 pass per `SingleOp`, in qvnt's own operand order; its amplitudes
+ *          are bit-identical to qvnt's non-fast-math arithmetic.  It is the plain f64 GPU path. */
+enum qvnt_engine { QVNT_ENGINE_FUSED = 0, QVNT_ENGINE_PLAIN = 1 };
+
+/* ---------------------------------------------------------------------------------------------
+ * Status / errors
+ * ------------------------------------------------------------------------------------------- */
+const char* qvnt_status_string(int status);
+/* Message of the last failing call on the calling thread ("" if none). */
+const char* qvnt_last_error(void);
+/* ABI version: (major << 16) | minor. */
+uint32_t qvnt_abi_version(void);
+
+/* ---------------------------------------------------------------------------------------------
+ * Context: one CUDA device.  Replaces the global Rayon pool (src/threads.rs:32-52).
+ * ------------------------------------------------------------------------------------------- */
+int qvnt_ctx_create(int device, qvnt_ctx** out);
+int qvnt_ctx_destroy(qvnt_ctx* ctx);
+/* Free device memory and the total in bytes, as the CUDA runtime reports them for this device. */
+int qvnt_ctx_mem_info(qvnt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
+
+/* ---------------------------------------------------------------------------------------------
+ * Registers (QReg, src/register/quant.rs:102-150)
+ * ------------------------------------------------------------------------------------------- */
+/* `QReg::with_state(q_num, state)`; `QReg::new(q_num)` is state = 0.  The state index is masked
+ * by 2^q_num - 1 as in quant.rs:131-142.  q_num <= 40. */
+int qvnt_reg_create(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, qvnt_reg** out);
+int qvnt_reg_destroy(qvnt_reg* reg);
+/* `QReg::clone` (derive(Clone), quant.rs:102). */
+int qvnt_reg_clone(const qvnt_reg* reg, qvnt_reg** out);
+/* `QReg::num` (quant.rs:152-154). */
+int qvnt_reg_num(const qvnt_reg* reg, uint32_t* q_num);
+/* Number of stored amplitudes, max(2^q_num, 8) (quant.rs:15, :116). */
+int qvnt_reg_len(const qvnt_reg* reg, uint64_t* len);
+/* Select the engine (enum qvnt_engine) that later qvnt_reg_apply calls use. */
+int qvnt_reg_set_engine(qvnt_reg* reg, int engine);
+/* Fused engine: tile width in qubits (0 = automatic).  Values outside [6, 13] are rejected. */
+int qvnt_reg_set_fusion_width(qvnt_reg* reg, uint32_t k);
+
+/* `QReg::apply(&MultiOp)` (quant.rs:376-395, multi/mod.rs:97-114): the gates run in order, each one
+ * over the whole register.  All gates are validated before any runs; an invalid gate returns
+ * QVNT_ERR_BAD_MASK or QVNT_ERR_BAD_ARG and leaves the state unchanged.  Asynchronous on the
+ * register's stream: errors raised by the device surface on the next synchronising call. */
+int qvnt_reg_apply(qvnt_reg* reg, const qvnt_gate* gates, size_t count);
+
+/* `QReg::measure_mask(mask)` (quant.rs:490-501) with the uniform draw injected by the caller:
+ * u01 in [0, 1) replaces `thread_rng()`.  The chosen index is the first i whose inclusive
+ * cumulative probability exceeds u01 * (sum of probabilities), qvnt's `WeightedIndex` rule.
+ * Collapses amplitudes with (i ^ idx) & mask != 0 to zero WITHOUT renormalising, as qvnt does.
+ * *out_value = idx & mask (`CReg::get`).  mask & (2^n - 1) == 0 returns 0 and leaves the state. */
+int qvnt_reg_measure_mask(qvnt_reg* reg, uint64_t mask, double u01, uint64_t* out_value);
+/* Same as qvnt_reg_measure_mask, then rescales the state to unit norm when renormalise != 0. */
+int qvnt_reg_measure_mask_ex(qvnt_reg* reg, uint64_t mask, double u01, int renormalise,
+                             uint64_t* out_value);
+
+/* `QReg::get_probabilities` (quant.rs:434-454): p_i = |psi_i|^2 * (1 / sum over the whole buffer),
+ * for i < 2^n.  host_out holds 2^n doubles. */
+int qvnt_reg_get_probabilities(qvnt_reg* reg, double* host_out);
+/* `QReg::get_absolute` (quant.rs:458-466): sum of |psi_i|^2 over the whole buffer. */
+int qvnt_reg_get_absolute(qvnt_reg* reg, double* out);
+/* `QReg::get_polar` (quant.rs:417-431): (|psi_i|, arg psi_i) for i < 2^n, interleaved, 2*2^n doubles. */
+int qvnt_reg_get_polar(qvnt_reg* reg, double* host_out);
+/* Copies all max(2^n, 8) amplitudes to the host, interleaved (re, im). */
+int qvnt_reg_get_amplitudes(qvnt_reg* reg, double* host_out);
+/* Copies amplitudes [first, first + count) to the host, interleaved (re, im): a slice of qvnt's
+ * `psi` without reading the whole state. */
+int qvnt_reg_get_amplitudes_range(qvnt_reg* reg, uint64_t first, uint64_t count, double* host_out);
+/* Replaces all max(2^n, 8) amplitudes from the host, interleaved (re, im). */
+int qvnt_reg_set_amplitudes(qvnt_reg* reg, const double* host_in);
+/* `QReg::reset(state)` (quant.rs:202-205): |state & q_mask>. */
+int qvnt_reg_reset(qvnt_reg* reg, uint64_t state);
+/* `QReg::reset_by_mask(mask)` (quant.rs:207-229): zero amplitudes with i & mask != 0, then
+ * `normalize` (quant.rs:397-414); mask covering all qubits resets to |0>. */
+int qvnt_reg_reset_by_mask(qvnt_reg* reg, uint64_t mask);
+/* `normalize` (quant.rs:397-414): norm <= 1e-15 resets to |0>; 1 - norm <= 1e-9 leaves the state. */
+int qvnt_reg_normalize(qvnt_reg* reg);
+/* Tensor product `QReg * QReg` (quant.rs:330-371): out = a (low qubits) x b (high qubits). */
+int qvnt_reg_tensor(const qvnt_reg* a, const qvnt_reg* b, qvnt_reg** out);
+/* Waits for all work queued on the register's stream. */
+int qvnt_reg_sync(qvnt_reg* reg);
+/* The register's cudaStream_t, for callers that order their own work (or timing events) after it. */
+int qvnt_reg_get_stream(const qvnt_reg* reg, void** stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Out-of-place plugin call: `Applicable::apply(&self, psi_i: &[C], psi_o: &mut Vec<C>)`
+ * (src/operator/applicable.rs:5-6).  psi_i and psi_o are host buffers of `len` interleaved
+ * complex doubles (len a power of two, >= 8); the call copies psi_i to the device, runs the gates
+ * on the context's scratch register and copies the result to psi_o before returning.
+ * ------------------------------------------------------------------------------------------- */
+int qvnt_apply_host(qvnt_ctx* ctx, const qvnt_gate* gates, size_t count, const double* psi_i,
+                    double* psi_o, uint64_t len);
+
+/* ---------------------------------------------------------------------------------------------
+ * Gate builders for hosts without qvnt's Rust `op::` (C, C++, Python).  A Rust host keeps its own
+ * `op::` and lowers `SingleOp`s itself.  List builders write at most `cap` gates to `out` and the
+ * full count to *count; call with cap = 0 to size the list.
+ * ------------------------------------------------------------------------------------------- */
+/* Checked single-gate constructor, the atomic `::new` + `is_valid` (single/mod.rs:4-11).
+ * angle is used by RX/RY/RZ/RXX/RYY/RZZ (stored as (cos(angle/2), sin(angle/2)));
+ * matrix (8 or 32 doubles) by U1/U2.  Invalid masks return QVNT_ERR_BAD_MASK. */
+int qvnt_gate_make(uint32_t kind, uint64_t a_mask, uint64_t b_mask, double angle,
+                   const double* matrix, qvnt_gate* out);
+/* `SingleOp::dgr` (single/mod.rs:97-103). */
+int qvnt_gate_dgr(qvnt_gate* gate);
+/* `SingleOp::c` (single/mod.rs:106-116): QVNT_ERR_BAD_MASK if c_mask overlaps act | ctrl. */
+int qvnt_gate_c(qvnt_gate* gate, uint64_t c_mask);
+/* `SingleOp::act_on` = act | ctrl (single/mod.rs:93-95). */
+uint64_t qvnt_gate_act_on(const qvnt_gate* gate);
+/* `SingleOp::name` (single/mod.rs:72-78), e.g. "C8_H3", "RX1(1.23456)".  Writes at most cap bytes
+ * including the terminator; *needed gets the full length without it. */
+int qvnt_gate_name(const qvnt_gate* gate, char* buf, size_t cap, size_t* needed);
+/* `op::h(mask)` (src/operator/multi/h.rs:14-45): H2 over pairs of set bits, then H1 if odd. */
+int qvnt_op_h(uint64_t mask, qvnt_gate* out, size_t cap, size_t* count);
+/* `op::qft(mask)` (src/operator/multi/qft.rs:4-33): H then controlled RZ(pi/2^j), no swaps. */
+int qvnt_op_qft(uint64_t mask, qvnt_gate* out, size_t cap, size_t* count);
+/* `op::qft_swapped(mask)` (src/operator/multi/qft.rs:35-52). */
+int qvnt_op_qft_swapped(uint64_t mask, qvnt_gate* out, size_t cap, size_t* count);
+/* `op::u2(phi, lam, mask)` = rz(lam) ry(pi/2) rz(phi) (src/operator/mod.rs:480-482), 3 gates. */
+int qvnt_op_u2(double phi, double lam, uint64_t mask, qvnt_gate* out, size_t cap, size_t* count);
+/* `op::u3(the, phi, lam, mask)` = rz(lam) ry(the) rz(phi) (src/operator/mod.rs:499-501), 3 gates. */
+int qvnt_op_u3(double the, double phi, double lam, uint64_t mask, qvnt_gate* out, size_t cap,
+               size_t* count);
+/* `MultiOp::dgr` (multi/mod.rs:120-123): reverses the list and daggers each gate, in place. */
+int qvnt_ops_dgr(qvnt_gate* gates, size_t count);
+/* `MultiOp::c` (multi/mod.rs:125-132): controls every gate; fails if c_mask overlaps act_on. */
+int qvnt_ops_c(qvnt_gate* gates, size_t count, uint64_t c_mask);
+
+/* ---------------------------------------------------------------------------------------------
+ * Counters for measurement: kernels launched and fused passes run by this register so far.
+ * ------------------------------------------------------------------------------------------- */
+int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* passes);
+/* Time the fused engine spends in its dominant kernel: CUDA events recorded around every launch of
+ * the fused-pass kernel on the register's stream since the last reset (enable != 0 turns
+ * recording on and clears the totals).  *ms = summed event time, *launches = number of launches. */
+int qvnt_reg_kernel_timing(qvnt_reg* reg, int enable, double* ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QVNT_GB300_H */

@@ -1,0 +1,18 @@
+"""qvnt_gb300: a GB300 (sm_103a) state-vector engine behind qvnt's register and operator API.
+
+    from qvnt_gb300 import QReg, op
+    q = QReg.with_state(10, 0b0011100000)
+    q.apply(op.qft(0b0000011111))
+    measured = q.measure_mask(0b0000000111)
+
+The state vector lives only in GPU memory; every gate, reduction and measurement runs in the
+library's CUDA kernels (qvnt_gb300/csrc/).  This package is the Python side of the C ABI in
+include/qvnt_gb300.h.
+"""
+from . import operator as op
+from ._abi import ENGINE_FUSED, ENGINE_PLAIN, KIND, KINDS, MaskError, QvntError, QvntGate
+from .operator import MultiOp, SingleOp
+from .register import Context, CReg, QReg, VReg, bits_iter, default_context
+
+__all__ = ["op", "QReg", "CReg", "VReg", "MultiOp", "SingleOp", "Context", "default_context", "bits_iter",
+           "QvntGate", "QvntError", "MaskError", "KIND", "KINDS", "ENGINE_FUSED", "ENGINE_PLAIN"]

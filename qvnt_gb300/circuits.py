@@ -1,0 +1,122 @@
+"""Seeded synthetic circuits: the workloads the engine is measured and checked on.
+
+There is no public circuit suite behind these; each generator draws from a SplitMix64 stream so
+that the GPU run, the CPU oracle and the CPU baseline see the same gate list.
+
+  plain_circuit(n=20, layers=20)   op::h(all), then per layer rx, ry, rz on every qubit with angles
+                                   in [0, 2pi) and nearest-neighbour CNOTs x(1<<(i+1)).c(1<<i) at an
+                                   alternating even/odd offset; then op::qft(all).  (~1,610 gates at
+                                   n = 20.)
+  random_circuit(n=30, depth=40)   per layer one gate from {h, s, t, u3(th, phi, lam)} on every
+                                   qubit, 15 two-qubit gates from {rxx, ryy, rzz, swap, i_swap,
+                                   sqrt_i_swap} on random distinct pairs, 3 Toffolis
+                                   x(t).c(c1 | c2); then op::qft(all).  (~2,985 gates at n = 30.)
+"""
+import math
+
+from . import operator as op
+from .operator import MultiOp
+
+_MASK64 = (1 << 64) - 1
+TWO_PI = 2.0 * math.pi
+
+
+class SplitMix64:
+    def __init__(self, seed):
+        self.state = seed & _MASK64
+
+    def next_u64(self):
+        self.state = (self.state + 0x9E3779B97F4A7C15) & _MASK64
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK64
+        return z ^ (z >> 31)
+
+    def uniform(self):
+        """Uniform double in [0, 1) with 53 random bits."""
+        return (self.next_u64() >> 11) * (1.0 / 9007199254740992.0)
+
+    def below(self, n):
+        return self.next_u64() % n
+
+
+def plain_circuit(n=20, layers=20, seed=1):
+    rng = SplitMix64(seed)
+    all_mask = (1 << n) - 1
+    ops = [op.h(all_mask)]
+    for layer in range(layers):
+        for q in range(n):
+            ops.append(op.rx(TWO_PI * rng.uniform(), 1 << q))
+            ops.append(op.ry(TWO_PI * rng.uniform(), 1 << q))
+            ops.append(op.rz(TWO_PI * rng.uniform(), 1 << q))
+        for i in range(layer % 2, n - 1, 2):
+            ops.append(op.x(1 << (i + 1)).c(1 << i))
+    ops.append(op.qft(all_mask))
+    return _concat(ops)
+
+
+def random_layers(n, depth, rng):
+    ops = []
+    for _ in range(depth):
+        for q in range(n):
+            kind = rng.below(4)
+            if kind == 0:
+                ops.append(op.h(1 << q))
+            elif kind == 1:
+                ops.append(op.s(1 << q))
+            elif kind == 2:
+                ops.append(op.t(1 << q))
+            else:
+                th, ph, la = TWO_PI * rng.uniform(), TWO_PI * rng.uniform(), TWO_PI * rng.uniform()
+                ops.append(op.u3(th, ph, la, 1 << q))
+        for _ in range(15):
+            a = rng.below(n)
+            b = rng.below(n - 1)
+            if b >= a:
+                b += 1
+            ab = (1 << a) | (1 << b)
+            kind = rng.below(6)
+            if kind < 3:
+                ops.append((op.rxx, op.ryy, op.rzz)[kind](TWO_PI * rng.uniform(), ab))
+            else:
+                ops.append((op.swap, op.i_swap, op.sqrt_i_swap)[kind - 3](ab))
+        for _ in range(3):
+            t = rng.below(n)
+            c1 = rng.below(n - 1)
+            if c1 >= t:
+                c1 += 1
+            c2 = rng.below(n)
+            while c2 == t or c2 == c1:
+                c2 = rng.below(n)
+            ops.append(op.x(1 << t).c((1 << c1) | (1 << c2)))
+    return ops
+
+
+def random_circuit(n=30, depth=40, seed=2, with_qft=True):
+    rng = SplitMix64(seed)
+    ops = random_layers(n, depth, rng)
+    if with_qft:
+        ops.append(op.qft((1 << n) - 1))
+    return _concat(ops)
+
+
+def inverse(circuit):
+    """The true inverse of a circuit.  qvnt's `.dgr()` maps a rotation R(theta) to -R(theta)
+    (its stored phase is negated, src/operator/atomic/rx.rs:42-47), so it is not an inverse for
+    rotations; here rotations are inverted by conjugating the stored phase instead."""
+    out = []
+    for s in reversed(circuit.ops):
+        g = s.clone()
+        if g.g.kind in (2, 3, 5, 6, 10, 11):  # RX RXX RY RYY RZ RZZ
+            g.g.phase[1] = -g.g.phase[1]
+        else:
+            g = g.dgr()
+        out.append(g)
+    return MultiOp(out)
+
+
+def _concat(ops):
+    r = MultiOp()
+    for o in ops:
+        r = r * o
+    return r

@@ -1,0 +1,71 @@
+// Internal structures shared by the C ABI (abi.cu) and the fused engine (fused.cu).
+#pragma once
+
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "common.cuh"
+
+namespace qvnt {
+
+// Fused-pass tile widths accepted by qvnt_reg_set_fusion_width.
+constexpr uint32_t kFusedMinK = 6;
+constexpr uint32_t kFusedMaxK = 13;
+
+// Device buffers the fused engine keeps between apply calls (pass descriptors, gate tables).
+struct FusedState {
+    void* d_buf = nullptr;
+    size_t d_bytes = 0;
+    void* h_buf = nullptr;  // pinned host mirror for the upload
+    size_t h_bytes = 0;
+    void release();
+};
+
+}  // namespace qvnt
+
+struct qvnt_ctx {
+    uint32_t magic = 0;
+    int device = 0;
+    qvnt::Geometry geo;
+    int smem_optin = 0;
+    int default_engine = QVNT_ENGINE_FUSED;
+    std::mutex host_mu;
+    struct qvnt_reg* host_reg = nullptr;  // scratch register of qvnt_apply_host
+};
+
+struct qvnt_reg {
+    uint32_t magic = 0;
+    qvnt_ctx* ctx = nullptr;
+    uint32_t q_num = 0;
+    uint64_t len = 0;  // max(2^q_num, 8) amplitudes
+    qvnt::amp_t* psi = nullptr;
+    qvnt::amp_t* alt = nullptr;  // lazily allocated second buffer (out-of-place passes)
+    double* scratch = nullptr;   // reduction partials
+    void* staging = nullptr;     // device staging for host reads
+    uint64_t staging_bytes = 0;
+    void* d_small = nullptr;     // 64 B of device results (index, status, sums)
+    void* h_small = nullptr;     // pinned 64 B host mirror
+    cudaStream_t stream = nullptr;
+    int engine = QVNT_ENGINE_FUSED;
+    uint32_t fusion_k = 0;
+    uint64_t launches = 0;
+    uint64_t passes = 0;
+    uint64_t last_measured_index = 0;
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
+    qvnt::FusedState fused;
+};
+
+namespace qvnt {
+int validate_gate(const qvnt_gate& g, uint64_t len);
+uint64_t gate_acts_on(const qvnt_gate& g);
+int gate_check_masks(const qvnt_gate& g);
+DevGate decode_gate(const qvnt_gate& g);
+int reg_ensure_alt(qvnt_reg* r);
+int timing_begin(qvnt_reg* r, cudaEvent_t* stop);
+int timing_end(qvnt_reg* r, cudaEvent_t stop);
+int apply_plain(qvnt_reg* r, const qvnt_gate* gates, size_t count);
+int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count);
+int launch_inv(const double* d_abs, double* d_inv, int* d_status, cudaStream_t stream);
+}  // namespace qvnt

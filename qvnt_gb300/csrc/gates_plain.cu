@@ -1,0 +1,177 @@
+// Plain engine: one in-place FP64 pass per SingleOp (the plain f64 GPU path).
+//
+// qvnt computes every output amplitude by a gather over the input (`AtomicOp::for_each`,
+// src/operator/atomic/dispatch.rs:32-67) into a second buffer.  Here each thread owns one ORBIT of
+// the gate -- the 1, 2 or 4 amplitudes that only read each other -- loads it once, evaluates the
+// same `atomic_op` expression for every member and stores the results in place.  Orbits are
+// enumerated by bit insertion: the target bits are inserted as 0 and the control bits as 1 into a
+// dense counter, so a gate with c controls touches only 2^(n-c) amplitudes.  Built with
+// --fmad=false: results are bit-identical to qvnt's non-fast-math arithmetic.
+#include <algorithm>
+#include <vector>
+
+#include "atomic.cuh"
+#include "kernels.h"
+
+namespace qvnt {
+
+namespace {
+
+constexpr int kUnroll = 2;
+
+template <int SHAPE>
+__global__ void __launch_bounds__(256) plain_gate_kernel(amp_t* __restrict__ psi, const DevGate g,
+                                                         const Enum e, const uint64_t pmask) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j0 < e.count; j0 += stride * kUnroll) {
+        amp_t v[kUnroll][SHAPE];
+        uint64_t base[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint64_t j = j0 + u * stride;
+            if (j < e.count) {
+                base[u] = enum_index(e, j);
+                if (SHAPE == 1) {
+                    v[u][0] = psi[base[u]];
+                } else if (SHAPE == 2) {
+                    v[u][0] = psi[base[u]];
+                    v[u][1] = psi[base[u] ^ pmask];
+                } else {
+                    v[u][0] = psi[base[u]];
+                    v[u][1] = psi[base[u] | g.a];
+                    v[u][2] = psi[base[u] | g.b];
+                    v[u][3] = psi[base[u] | g.a | g.b];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const uint64_t j = j0 + u * stride;
+            if (j >= e.count) continue;
+            const uint64_t i0 = base[u];
+            if (SHAPE == 1) {
+                const amp_t x = v[u][0];
+                psi[i0] = atomic_op(g, i0, [&](uint64_t) { return x; });
+            } else if (SHAPE == 2) {
+                const amp_t x0 = v[u][0], x1 = v[u][1];
+                const uint64_t i1 = i0 ^ pmask;
+                auto f = [&](uint64_t k) { return k == i0 ? x0 : x1; };
+                const amp_t o0 = atomic_op(g, i0, f);
+                const amp_t o1 = atomic_op(g, i1, f);
+                psi[i0] = o0;
+                psi[i1] = o1;
+            } else {
+                const amp_t x0 = v[u][0], x1 = v[u][1], x2 = v[u][2], x3 = v[u][3];
+                const uint64_t a = g.a, b = g.b;
+                auto f = [&](uint64_t k) {
+                    const int s = ((k & a) ? 1 : 0) | ((k & b) ? 2 : 0);
+                    return s == 0 ? x0 : (s == 1 ? x1 : (s == 2 ? x2 : x3));
+                };
+                const amp_t o0 = atomic_op(g, i0, f);
+                const amp_t o1 = atomic_op(g, i0 | a, f);
+                const amp_t o2 = atomic_op(g, i0 | b, f);
+                const amp_t o3 = atomic_op(g, i0 | a | b, f);
+                psi[i0] = o0;
+                psi[i0 | a] = o1;
+                psi[i0 | b] = o2;
+                psi[i0 | a | b] = o3;
+            }
+        }
+    }
+}
+
+// qvnt's own out-of-place gather, for gates whose orbits are not closed (a U2 controlled on its
+// own b qubit, which qvnt allows because u2 `acts_on` omits b_mask, u2.rs:70-72).
+__global__ void __launch_bounds__(256) gather_gate_kernel(const amp_t* __restrict__ in, amp_t* __restrict__ out,
+                                                          const DevGate g, const uint64_t len) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < len; idx += stride) {
+        if ((~idx & g.ctrl) == 0)
+            out[idx] = atomic_op(g, idx, [&](uint64_t k) { return in[k]; });
+        else
+            out[idx] = in[idx];
+    }
+}
+
+inline int high_bit(uint64_t m) { return 63 - __builtin_clzll(m); }
+inline int low_bit(uint64_t m) { return __builtin_ctzll(m); }
+
+Enum make_enum(uint64_t len, uint64_t inserted, uint64_t ones) {
+    Enum e{};
+    std::vector<uint32_t> pos;
+    for (int p = 0; p < 64; ++p)
+        if ((inserted >> p) & 1ull) pos.push_back((uint32_t)p);
+    e.nins = (uint32_t)pos.size();
+    for (size_t k = 0; k < pos.size(); ++k) e.ins[k] = pos[k];
+    e.ones = ones;
+    e.count = len >> pos.size();
+    return e;
+}
+
+unsigned grid_for(uint64_t work, const Geometry& geo, int threads) {
+    uint64_t want = (work + (uint64_t)threads * kUnroll - 1) / ((uint64_t)threads * kUnroll);
+    uint64_t cap = (uint64_t)geo.sms * geo.blocks_per_sm;
+    if (want > cap) want = cap;
+    if (want < 1) want = 1;
+    return (unsigned)want;
+}
+
+}  // namespace
+
+bool plain_gate_is_identity(const DevGate& g) {
+    switch (g.kind) {
+    case QVNT_GATE_ID:
+        return true;
+    case QVNT_GATE_X: case QVNT_GATE_Y: case QVNT_GATE_Z: case QVNT_GATE_S: case QVNT_GATE_T:
+        return g.a == 0;  // popcount(idx & 0) = 0 everywhere: every output equals its input
+    default:
+        return false;
+    }
+}
+
+bool plain_gate_needs_gather(const DevGate& g) { return g.kind == QVNT_GATE_U2 && (g.ctrl & g.b) != 0; }
+
+int launch_plain_gate(amp_t* psi, uint64_t len, const DevGate& g, cudaStream_t stream, const Geometry& geo) {
+    const int threads = 256;
+    const uint64_t ctrl = g.ctrl;
+    switch (g.kind) {
+    case QVNT_GATE_Z: case QVNT_GATE_S: case QVNT_GATE_T: case QVNT_GATE_RZ: case QVNT_GATE_RZZ: {
+        Enum e = make_enum(len, ctrl, ctrl);
+        plain_gate_kernel<1><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, 0);
+        break;
+    }
+    case QVNT_GATE_X: case QVNT_GATE_Y: case QVNT_GATE_RX: case QVNT_GATE_RY: case QVNT_GATE_H1:
+    case QVNT_GATE_U1: case QVNT_GATE_RXX: case QVNT_GATE_RYY: {
+        const uint64_t pivot = 1ull << high_bit(g.a);
+        Enum e = make_enum(len, ctrl | pivot, ctrl);
+        plain_gate_kernel<2><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, g.a);
+        break;
+    }
+    case QVNT_GATE_SWAP: case QVNT_GATE_ISWAP: case QVNT_GATE_SQRT_SWAP: case QVNT_GATE_SQRT_ISWAP: {
+        // Only members with odd parity of idx & ab change (swap.rs:17): pair (01) <-> (10).
+        const uint64_t lo = 1ull << low_bit(g.a);
+        Enum e = make_enum(len, ctrl | g.a, ctrl | lo);
+        plain_gate_kernel<2><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, g.a);
+        break;
+    }
+    case QVNT_GATE_H2: case QVNT_GATE_U2: {
+        Enum e = make_enum(len, ctrl | g.a | g.b, ctrl);
+        plain_gate_kernel<4><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, 0);
+        break;
+    }
+    default:
+        return QVNT_OK;
+    }
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_gather_gate(const amp_t* in, amp_t* out, uint64_t len, const DevGate& g, cudaStream_t stream,
+                       const Geometry& geo) {
+    const int threads = 256;
+    gather_gate_kernel<<<grid_for(len, geo, threads), threads, 0, stream>>>(in, out, g, len);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+}  // namespace qvnt

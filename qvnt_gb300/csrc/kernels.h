@@ -1,0 +1,43 @@
+// Host-side launch functions of the engine's kernels.  All run asynchronously on `stream`.
+#pragma once
+
+#include "common.cuh"
+
+namespace qvnt {
+
+// ---- plain engine (gates_plain.cu) ----
+bool plain_gate_is_identity(const DevGate& g);
+bool plain_gate_needs_gather(const DevGate& g);
+int launch_plain_gate(amp_t* psi, uint64_t len, const DevGate& g, cudaStream_t stream, const Geometry& geo);
+int launch_gather_gate(const amp_t* in, amp_t* out, uint64_t len, const DevGate& g, cudaStream_t stream,
+                       const Geometry& geo);
+
+// ---- reductions, measurement and register-wide passes (measure.cu) ----
+// Number of amplitudes one reduction block covers; partial-sum buffers hold len / kChunk entries.
+constexpr uint64_t kChunk = 4096;
+inline uint64_t chunk_count(uint64_t len) { return (len + kChunk - 1) / kChunk; }
+
+// Sum of |psi_i|^2 over [0, len) into *d_out (device), deterministic order.  scratch: chunk_count(len)
+// doubles.
+int launch_norm_sqr_sum(const amp_t* psi, uint64_t len, double* scratch, double* d_out, cudaStream_t stream);
+// Full measure_mask on the device: the result index goes to *d_idx (device, 1 uint64).
+// scratch: 2 * chunk_count(len) + 8 doubles.  *d_status (device int) gets QVNT_ERR_BAD_ARG when the
+// state has zero norm.
+int launch_measure(amp_t* psi, uint64_t len, uint64_t q_size, uint64_t mask, double u01, double* scratch,
+                   uint64_t* d_idx, int* d_status, int renormalise, cudaStream_t stream);
+// p_i = |psi_i|^2 * inv_abs for i in [first, first + count), to d_out.
+int launch_probabilities(const amp_t* psi, uint64_t first, uint64_t count, const double* d_inv_abs,
+                         double* d_out, cudaStream_t stream);
+// (|psi_i|, arg psi_i) for i in [first, first + count), interleaved to d_out.
+int launch_polar(const amp_t* psi, uint64_t first, uint64_t count, double* d_out, cudaStream_t stream);
+// psi = |state>.
+int launch_reset(amp_t* psi, uint64_t len, uint64_t state, cudaStream_t stream);
+// psi_i = 0 where i & mask != 0.
+int launch_zero_mask(amp_t* psi, uint64_t len, uint64_t mask, cudaStream_t stream);
+// `normalize` (quant.rs:397-414) given d_abs = sum |psi|^2 on the device.
+int launch_normalize(amp_t* psi, uint64_t len, const double* d_abs, cudaStream_t stream);
+// out_i = a[i & ma] * b[(i >> na) & mb] for i < 2^(na+nb), 0 above (quant.rs:330-371).
+int launch_tensor(const amp_t* a, uint32_t na, const amp_t* b, uint32_t nb, amp_t* out, uint64_t out_len,
+                  cudaStream_t stream);
+
+}  // namespace qvnt

@@ -1,0 +1,335 @@
+// Register-wide passes: norm, probabilities, measure_mask, collapse, normalize, reset, tensor.
+//
+// Built with --fmad=false so that |psi|^2 = re*re + im*im and p_i = |psi_i|^2 * (1/sum) round as
+// qvnt's `norm_sqr` and `get_probabilities` do (src/register/quant.rs:434-454).  Sums are taken in
+// a fixed tree order (chunk partials, then one block), so every result is reproducible run to run.
+#include <math.h>
+
+#include "atomic.cuh"
+#include "kernels.h"
+
+namespace qvnt {
+
+namespace {
+
+constexpr int kRedThreads = 256;   // chunk reduction block
+constexpr int kScanThreads = 1024; // single-block search
+
+__device__ __forceinline__ double nsq(amp_t z) { return z.x * z.x + z.y * z.y; }
+
+template <int THREADS>
+__device__ __forceinline__ double block_sum(double v, double* sm) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sm[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = (l < THREADS / 32) ? sm[l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;  // valid in thread 0
+}
+
+// Inclusive scan over the block in thread order; returns this thread's inclusive prefix and the
+// block total in *total.
+template <int THREADS>
+__device__ __forceinline__ double block_inclusive_scan(double v, double* sm, double* total) {
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double u = __shfl_up_sync(0xffffffffu, v, o);
+        if (l >= o) v += u;
+    }
+    __syncthreads();
+    if (l == 31) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double s = (l < THREADS / 32) ? sm[l] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double u = __shfl_up_sync(0xffffffffu, s, o);
+            if (l >= o) s += u;
+        }
+        if (l < THREADS / 32) sm[l] = s;
+    }
+    __syncthreads();
+    if (w > 0) v += sm[w - 1];
+    *total = sm[THREADS / 32 - 1];
+    return v;
+}
+
+// Partial sums per chunk of kChunk amplitudes: sum_i |psi_i|^2 * scale over i < limit.
+__global__ void __launch_bounds__(kRedThreads) chunk_sum_kernel(const amp_t* __restrict__ psi, uint64_t limit,
+                                                                 const double* __restrict__ d_scale,
+                                                                 double* __restrict__ partial) {
+    __shared__ double sm[32];
+    const uint64_t base = (uint64_t)blockIdx.x * kChunk;
+    const double scale = d_scale ? *d_scale : 1.0;
+    double s = 0.0;
+    for (uint32_t k = threadIdx.x; k < kChunk; k += kRedThreads) {
+        const uint64_t i = base + k;
+        if (i < limit) s += d_scale ? nsq(psi[i]) * scale : nsq(psi[i]);
+    }
+    double t = block_sum<kRedThreads>(s, sm);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(kScanThreads) final_sum_kernel(const double* __restrict__ partial, uint64_t n,
+                                                                  double* __restrict__ out) {
+    __shared__ double sm[32];
+    double s = 0.0;
+    for (uint64_t k = threadIdx.x; k < n; k += kScanThreads) s += partial[k];
+    double t = block_sum<kScanThreads>(s, sm);
+    if (threadIdx.x == 0) *out = t;
+}
+
+// inv = 1/abs; flags a zero or non-finite norm (qvnt's WeightedIndex::new(..).unwrap() panics).
+__global__ void inv_kernel(const double* d_abs, double* d_inv, int* d_status) {
+    const double a = *d_abs;
+    *d_inv = 1. / a;
+    if (!(a > 0.0) || !isfinite(1. / a)) *d_status = QVNT_ERR_BAD_ARG;
+}
+
+// WeightedIndex selection (rand 0.8.5): first i with inclusive cumulative p > u01 * total,
+// i <= q_size - 2, else q_size - 1.  One block: chunk-level prefix, then element-level prefix
+// inside the crossing chunk.
+__global__ void __launch_bounds__(kScanThreads) search_kernel(const amp_t* __restrict__ psi, uint64_t q_size,
+                                                               const double* __restrict__ pchunk,
+                                                               const double* __restrict__ d_inv, double u01,
+                                                               uint64_t* __restrict__ d_idx) {
+    __shared__ double sm[32];
+    __shared__ double s_incl[kScanThreads];
+    __shared__ unsigned long long s_found;
+    __shared__ double s_before;
+    __shared__ double s_chosen;
+    const int t = threadIdx.x;
+    const uint64_t nq = (q_size + kChunk - 1) / kChunk;
+    const uint64_t per = (nq + kScanThreads - 1) / kScanThreads;
+    const uint64_t c0 = (uint64_t)t * per;
+    double local = 0.0;
+    for (uint64_t c = c0; c < c0 + per && c < nq; ++c) local += pchunk[c];
+    double total;
+    const double incl = block_inclusive_scan<kScanThreads>(local, sm, &total);
+    s_incl[t] = incl;
+    if (t == 0) {
+        s_found = ~0ull;
+        s_chosen = u01 * total;
+    }
+    __syncthreads();
+    const double chosen = s_chosen;
+    const double excl = t ? s_incl[t - 1] : 0.0;
+    // The first thread whose range crosses `chosen` scans its chunks.
+    if (incl > chosen && !(excl > chosen)) {
+        double run = excl;
+        for (uint64_t c = c0; c < c0 + per && c < nq; ++c) {
+            const double nxt = run + pchunk[c];
+            if (nxt > chosen) {
+                s_found = (unsigned long long)c;
+                s_before = run;
+                break;
+            }
+            run = nxt;
+        }
+    }
+    __syncthreads();
+    const unsigned long long chunk = s_found;
+    if (chunk == ~0ull) {
+        if (t == 0) *d_idx = q_size - 1;
+        return;
+    }
+    const double before = s_before;
+    const double inv = *d_inv;
+    // Element level: thread t owns kChunk / kScanThreads contiguous amplitudes of the chunk.
+    constexpr int per_t = (int)(kChunk / kScanThreads);
+    const uint64_t e0 = (uint64_t)chunk * kChunk + (uint64_t)t * per_t;
+    double p[per_t];
+    double ls = 0.0;
+#pragma unroll
+    for (int k = 0; k < per_t; ++k) {
+        const uint64_t i = e0 + k;
+        p[k] = (i < q_size) ? nsq(psi[i]) * inv : 0.0;
+        ls += p[k];
+    }
+    __syncthreads();
+    double tot2;
+    const double incl2 = block_inclusive_scan<kScanThreads>(ls, sm, &tot2);
+    __syncthreads();
+    s_incl[t] = incl2;
+    if (t == 0) s_found = ~0ull;
+    __syncthreads();
+    double run = before + (t ? s_incl[t - 1] : 0.0);
+#pragma unroll
+    for (int k = 0; k < per_t; ++k) {
+        run += p[k];
+        const uint64_t i = e0 + k;
+        if (i < q_size && run > chosen) {
+            atomicMin(&s_found, (unsigned long long)i);
+            break;
+        }
+    }
+    __syncthreads();
+    if (t == 0) {
+        unsigned long long f = s_found;
+        if (f == ~0ull) {
+            // The chunk total and its element prefix differ by rounding only: take the chunk's last
+            // index (the boundary lies within an ulp of `chosen`).
+            uint64_t last = (uint64_t)chunk * kChunk + kChunk - 1;
+            f = last < q_size ? last : q_size - 1;
+        }
+        if (f > q_size - 2) f = q_size - 1;  // cumulative_weights has q_size - 1 entries
+        *d_idx = f;
+    }
+}
+
+__global__ void collapse_kernel(amp_t* __restrict__ psi, uint64_t len, const uint64_t* __restrict__ d_idx,
+                                uint64_t mask) {
+    const uint64_t idy = *d_idx;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        if (((i ^ idy) & mask) != 0) psi[i] = make_double2(0.0, 0.0);
+}
+
+__global__ void scale_kernel(amp_t* __restrict__ psi, uint64_t len, const double* __restrict__ d_abs, int mode) {
+    // mode 0: qvnt `normalize` thresholds; mode 1: always rescale to unit norm (renormalise).
+    const double norm = sqrt(*d_abs);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    if (norm <= 1e-15) {
+        if (mode == 1) return;
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+            psi[i] = make_double2(i == 0 ? 1.0 : 0.0, 0.0);
+        return;
+    }
+    if (mode == 0 && 1. - norm <= 1e-9) return;
+    const double inv = 1. / norm;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride) {
+        amp_t v = psi[i];
+        psi[i] = make_double2(v.x * inv, v.y * inv);
+    }
+}
+
+__global__ void prob_kernel(const amp_t* __restrict__ psi, uint64_t first, uint64_t count,
+                            const double* __restrict__ d_inv, double* __restrict__ out) {
+    const double inv = *d_inv;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride)
+        out[k] = nsq(psi[first + k]) * inv;
+}
+
+__global__ void polar_kernel(const amp_t* __restrict__ psi, uint64_t first, uint64_t count, double* __restrict__ out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+        amp_t v = psi[first + k];
+        out[2 * k] = hypot(v.x, v.y);
+        out[2 * k + 1] = atan2(v.y, v.x);
+    }
+}
+
+__global__ void reset_kernel(amp_t* __restrict__ psi, uint64_t len, uint64_t state) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        psi[i] = make_double2(i == state ? 1.0 : 0.0, 0.0);
+}
+
+__global__ void zero_mask_kernel(amp_t* __restrict__ psi, uint64_t len, uint64_t mask) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        if (i & mask) psi[i] = make_double2(0.0, 0.0);
+}
+
+__global__ void tensor_kernel(const amp_t* __restrict__ a, uint32_t na, const amp_t* __restrict__ b, uint32_t nb,
+                              amp_t* __restrict__ out, uint64_t out_len) {
+    const uint64_t q_size = 1ull << (na + nb);
+    const uint64_t ma = (1ull << na) - 1, mb = (1ull << nb) - 1;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < out_len; i += stride)
+        out[i] = i < q_size ? c_mul(a[i & ma], b[(i >> na) & mb]) : make_double2(0.0, 0.0);
+}
+
+unsigned flat_grid(uint64_t n) {
+    uint64_t g = (n + 255) / 256;
+    const uint64_t cap = 152ull * 16;
+    if (g > cap) g = cap;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+int launch_norm_sqr_sum(const amp_t* psi, uint64_t len, double* scratch, double* d_out, cudaStream_t stream) {
+    const uint64_t nc = chunk_count(len);
+    chunk_sum_kernel<<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, scratch);
+    final_sum_kernel<<<1, kScanThreads, 0, stream>>>(scratch, nc, d_out);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_measure(amp_t* psi, uint64_t len, uint64_t q_size, uint64_t mask, double u01, double* scratch,
+                   uint64_t* d_idx, int* d_status, int renormalise, cudaStream_t stream) {
+    const uint64_t nc = chunk_count(len);
+    double* partial = scratch;
+    double* pchunk = scratch + nc;
+    double* d_abs = scratch + 2 * nc;
+    double* d_inv = d_abs + 1;
+    chunk_sum_kernel<<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, partial);
+    final_sum_kernel<<<1, kScanThreads, 0, stream>>>(partial, nc, d_abs);
+    inv_kernel<<<1, 1, 0, stream>>>(d_abs, d_inv, d_status);
+    chunk_sum_kernel<<<(unsigned)chunk_count(q_size), kRedThreads, 0, stream>>>(psi, q_size, d_inv, pchunk);
+    search_kernel<<<1, kScanThreads, 0, stream>>>(psi, q_size, pchunk, d_inv, u01, d_idx);
+    collapse_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, d_idx, mask);
+    if (renormalise) {
+        chunk_sum_kernel<<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, partial);
+        final_sum_kernel<<<1, kScanThreads, 0, stream>>>(partial, nc, d_abs);
+        scale_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, d_abs, 1);
+    }
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_probabilities(const amp_t* psi, uint64_t first, uint64_t count, const double* d_inv_abs,
+                         double* d_out, cudaStream_t stream) {
+    prob_kernel<<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_inv_abs, d_out);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_inv(const double* d_abs, double* d_inv, int* d_status, cudaStream_t stream) {
+    inv_kernel<<<1, 1, 0, stream>>>(d_abs, d_inv, d_status);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_polar(const amp_t* psi, uint64_t first, uint64_t count, double* d_out, cudaStream_t stream) {
+    polar_kernel<<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_out);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_reset(amp_t* psi, uint64_t len, uint64_t state, cudaStream_t stream) {
+    reset_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, state);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_zero_mask(amp_t* psi, uint64_t len, uint64_t mask, cudaStream_t stream) {
+    zero_mask_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, mask);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_normalize(amp_t* psi, uint64_t len, const double* d_abs, cudaStream_t stream) {
+    scale_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, d_abs, 0);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_tensor(const amp_t* a, uint32_t na, const amp_t* b, uint32_t nb, amp_t* out, uint64_t out_len,
+                  cudaStream_t stream) {
+    tensor_kernel<<<flat_grid(out_len), 256, 0, stream>>>(a, na, b, nb, out, out_len);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+}  // namespace qvnt

@@ -1,0 +1,191 @@
+"""ctypes binding of the CPU oracle (oracle/qvnt_oracle.c): TEST INFRASTRUCTURE ONLY.
+
+The oracle restates qvnt 0.4.4's arithmetic; the tests, the smoke check and the CPU-baseline leg of
+the benchmark use it as the checker.  Built by oracle/Makefile into oracle/_build/.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from qvnt_gb300._abi import KIND, QvntGate
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB = os.path.join(ORACLE_DIR, "_build", "libqvnt_oracle.so")
+
+_lib = None
+P = ctypes.POINTER
+c_u32, c_u64, c_int, c_double, c_size, c_void = (ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_double,
+                                                 ctypes.c_size_t, ctypes.c_void_p)
+
+_PROTOS = {
+    "oracle_acts_on": (c_u64, [P(QvntGate)]),
+    "oracle_apply": (None, [P(QvntGate), c_size, c_void, c_void, c_u64, c_int]),
+    "oracle_reg_len": (c_u64, [c_u32]),
+    "oracle_reg_init": (None, [c_u32, c_u64, c_void]),
+    "oracle_get_absolute": (c_double, [c_void, c_u64]),
+    "oracle_get_probabilities": (None, [c_void, c_u64, c_u32, c_void]),
+    "oracle_weighted_index": (c_u64, [c_void, c_u64, c_double]),
+    "oracle_collapse_mask": (None, [c_void, c_u64, c_u64, c_u64]),
+    "oracle_measure_mask": (c_u64, [c_void, c_u64, c_u32, c_u64, c_double, P(c_u64)]),
+    "oracle_reset": (None, [c_void, c_u64, c_u32, c_u64]),
+    "oracle_normalize": (None, [c_void, c_u64, c_u32]),
+    "oracle_reset_by_mask": (None, [c_void, c_u64, c_u32, c_u64]),
+    "oracle_get_polar": (None, [c_void, c_u32, c_void]),
+    "oracle_tensor": (None, [c_void, c_u32, c_void, c_u32, c_void]),
+    "oracle_gate_make": (c_int, [c_u32, c_u64, c_u64, c_double, P(c_double), P(QvntGate)]),
+    "oracle_is_unitary_m1": (c_int, [P(c_double)]),
+    "oracle_is_unitary_m2": (c_int, [P(c_double)]),
+    "oracle_gate_dgr": (None, [P(QvntGate)]),
+    "oracle_gate_c": (c_int, [P(QvntGate), c_u64]),
+    "oracle_op_h": (c_size, [c_u64, P(QvntGate)]),
+    "oracle_op_qft": (c_size, [c_u64, P(QvntGate)]),
+    "oracle_op_qft_swapped": (c_size, [c_u64, P(QvntGate)]),
+    "oracle_op_u3": (c_size, [c_double, c_double, c_double, c_u64, P(QvntGate)]),
+    "oracle_ops_dgr": (None, [P(QvntGate), c_size]),
+    "oracle_matrix": (None, [P(QvntGate), c_size, c_u32, c_void]),
+    "oracle_max_threads": (c_int, []),
+}
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        for name, (res, args) in _PROTOS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def arr(gates):
+    a = (QvntGate * max(len(gates), 1))()
+    for i, g in enumerate(gates):
+        a[i] = g
+    return a
+
+
+def make(kind, a=0, b=0, angle=0.0, matrix=None):
+    g = QvntGate()
+    m = None
+    if matrix is not None:
+        m = (ctypes.c_double * len(matrix))(*matrix)
+    st = lib().oracle_gate_make(KIND[kind], a, b, float(angle), m, ctypes.byref(g))
+    return g if st == 0 else None
+
+
+def dgr(g):
+    h = QvntGate.from_buffer_copy(g)
+    lib().oracle_gate_dgr(ctypes.byref(h))
+    return h
+
+
+def c(g, mask):
+    h = QvntGate.from_buffer_copy(g)
+    return h if lib().oracle_gate_c(ctypes.byref(h), mask) == 0 else None
+
+
+def _lst(fn, *args):
+    n = fn(*args, None)
+    a = (QvntGate * max(n, 1))()
+    fn(*args, a)
+    return [QvntGate.from_buffer_copy(a[i]) for i in range(n)]
+
+
+def op_h(mask):
+    return _lst(lib().oracle_op_h, mask)
+
+
+def op_qft(mask):
+    return _lst(lib().oracle_op_qft, mask)
+
+
+def op_qft_swapped(mask):
+    return _lst(lib().oracle_op_qft_swapped, mask)
+
+
+def op_u3(the, phi, lam, mask):
+    return _lst(lib().oracle_op_u3, float(the), float(phi), float(lam), mask)
+
+
+def reg_len(n):
+    return lib().oracle_reg_len(n)
+
+
+def new_state(n, state=0):
+    psi = np.zeros(reg_len(n), dtype=np.complex128)
+    lib().oracle_reg_init(n, state, psi.ctypes.data)
+    return psi
+
+
+def apply(gates, psi, nthreads=None):
+    """MultiOp::apply on a complex128 buffer, in place (one out-of-place pass per gate)."""
+    nthreads = nthreads or lib().oracle_max_threads()
+    scratch = np.empty_like(psi)
+    a = arr(gates)
+    lib().oracle_apply(a, len(gates), psi.ctypes.data, scratch.ctypes.data, psi.size, nthreads)
+    return psi
+
+
+def matrix(gates, size):
+    out = np.empty((1 << size, 1 << size), dtype=np.complex128)
+    lib().oracle_matrix(arr(gates), len(gates), size, out.ctypes.data)
+    return out
+
+
+def get_absolute(psi):
+    return lib().oracle_get_absolute(psi.ctypes.data, psi.size)
+
+
+def get_probabilities(psi, n):
+    out = np.empty(1 << n, dtype=np.float64)
+    lib().oracle_get_probabilities(psi.ctypes.data, psi.size, n, out.ctypes.data)
+    return out
+
+
+def weighted_index(w, u01):
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    return lib().oracle_weighted_index(w.ctypes.data, w.size, float(u01))
+
+
+def measure_mask(psi, n, mask, u01):
+    """Returns (CReg value, chosen index); collapses psi in place."""
+    idx = ctypes.c_uint64()
+    v = lib().oracle_measure_mask(psi.ctypes.data, psi.size, n, mask, float(u01), ctypes.byref(idx))
+    return v, idx.value
+
+
+def normalize(psi, n):
+    lib().oracle_normalize(psi.ctypes.data, psi.size, n)
+    return psi
+
+
+def reset_by_mask(psi, n, mask):
+    lib().oracle_reset_by_mask(psi.ctypes.data, psi.size, n, mask)
+    return psi
+
+
+def get_polar(psi, n):
+    out = np.empty((1 << n, 2), dtype=np.float64)
+    lib().oracle_get_polar(psi.ctypes.data, n, out.ctypes.data)
+    return out
+
+
+def tensor(a, na, b, nb):
+    out = np.empty(reg_len(na + nb), dtype=np.complex128)
+    lib().oracle_tensor(a.ctypes.data, na, b.ctypes.data, nb, out.ctypes.data)
+    return out
+
+
+def max_threads():
+    return lib().oracle_max_threads()
