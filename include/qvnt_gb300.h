@@ -227,6 +227,12 @@ int qvnt_ops_dgr(qvnt_gate* gates, size_t count);
 /* `MultiOp::c` (multi/mod.rs:125-132): controls every gate; fails if c_mask overlaps act_on. */
 int qvnt_ops_c(qvnt_gate* gates, size_t count, uint64_t c_mask);
 
+/* Plans a gate list for a q_num-qubit register on the fused engine without running it (host only,
+ * no device work): the number of passes (HBM round trips), register stages and engine gates it
+ * lowers to.  fusion_k as for qvnt_reg_set_fusion_width (0 = automatic). */
+int qvnt_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint32_t fusion_k, uint64_t* passes,
+                   uint64_t* stages, uint64_t* engine_gates);
+
 /* ---------------------------------------------------------------------------------------------
  * Counters for measurement: kernels launched and fused passes run by this register so far.
  * ------------------------------------------------------------------------------------------- */

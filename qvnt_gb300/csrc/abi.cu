@@ -117,6 +117,7 @@ int reg_alloc(qvnt_reg* r) {
         return set_cuda_error(e, "cudaMalloc(scratch)");
     }
     QVNT_CUDA_TRY(cudaMalloc(&r->d_small, 64));
+    QVNT_CUDA_TRY(cudaMemsetAsync(r->d_small, 0, 64, r->stream));
     QVNT_CUDA_TRY(cudaMallocHost(&r->h_small, 64));
     return QVNT_OK;
 }
@@ -161,8 +162,32 @@ int reg_ensure_staging(qvnt_reg* r, uint64_t bytes) {
     return QVNT_OK;
 }
 
+// Device-side error flag (d_small + 32): set by a fused kernel whose bounded wait ran out.
+int reg_check_device_error(qvnt_reg* r) {
+    int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
+    int* h_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->h_small) + 32);
+    QVNT_CUDA_TRY(cudaMemcpyAsync(h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, r->stream));
+    QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));
+    if (*h_err) {
+        *h_err = 0;
+        QVNT_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), r->stream));
+        return set_error(QVNT_ERR_TIMEOUT, "a fused pass gave up waiting for its tile copy; the state is invalid");
+    }
+    return QVNT_OK;
+}
+
 int reg_sync(qvnt_reg* r) {
     QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return reg_check_device_error(r);
+}
+
+// Storage format follows the engine: PLAIN keeps IEEE f64, FUSED keeps double-float pairs.
+int reg_set_format(qvnt_reg* r, int fmt) {
+    if (r->fmt == fmt) return QVNT_OK;
+    int st = launch_convert(r->psi, r->len, fmt == FMT_DF64 ? 1 : 0, r->stream);
+    if (st) return st;
+    r->fmt = fmt;
+    r->launches += 1;
     return QVNT_OK;
 }
 
@@ -194,10 +219,10 @@ int apply_plain(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
         if (plain_gate_needs_gather(d)) {
             st = reg_ensure_alt(r);
             if (st) return st;
-            st = launch_gather_gate(r->psi, r->alt, r->len, d, r->stream, r->ctx->geo);
+            st = launch_gather_gate(r->psi, r->alt, r->fmt, r->len, d, r->stream, r->ctx->geo);
             std::swap(r->psi, r->alt);
         } else {
-            st = launch_plain_gate(r->psi, r->len, d, r->stream, r->ctx->geo);
+            st = launch_plain_gate(r->psi, r->fmt, r->len, d, r->stream, r->ctx->geo);
         }
         if (st) return st;
         st = timing_end(r, stop);
@@ -243,6 +268,7 @@ int make_reg(qvnt_ctx* ctx, uint32_t q_num, qvnt_reg** out) {
     r->q_num = q_num;
     r->len = reg_len_for(q_num);
     r->engine = ctx->default_engine;
+    r->fmt = r->engine == QVNT_ENGINE_PLAIN ? FMT_F64 : FMT_DF64;
     int st = reg_alloc(r);
     if (st) {
         std::string msg = qvnt_last_error();
@@ -318,7 +344,7 @@ int qvnt_reg_create(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, qvnt_reg** ou
     qvnt_reg* r = nullptr;
     TRY(make_reg(ctx, q_num, &r));
     const uint64_t q_mask = (1ull << q_num) - 1;
-    int st = launch_reset(r->psi, r->len, state & q_mask, r->stream);  // quant.rs:129-150
+    int st = launch_reset(r->psi, r->fmt, r->len, state & q_mask, r->stream);  // quant.rs:129-150
     if (st) {
         reg_free(r);
         return st;
@@ -339,6 +365,7 @@ int qvnt_reg_clone(const qvnt_reg* reg, qvnt_reg** out) {
     qvnt_reg* r = nullptr;
     TRY(make_reg(reg->ctx, reg->q_num, &r));
     r->engine = reg->engine;
+    r->fmt = reg->fmt;
     r->fusion_k = reg->fusion_k;
     cudaError_t e = cudaStreamSynchronize(reg->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r->psi, reg->psi, r->len * sizeof(amp_t), cudaMemcpyDeviceToDevice, r->stream);
@@ -368,6 +395,8 @@ int qvnt_reg_set_engine(qvnt_reg* reg, int engine) {
     CHECK_REG(reg);
     if (engine != QVNT_ENGINE_FUSED && engine != QVNT_ENGINE_PLAIN)
         return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
+    QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
+    TRY(reg_set_format(reg, engine == QVNT_ENGINE_PLAIN ? FMT_F64 : FMT_DF64));
     reg->engine = engine;
     return QVNT_OK;
 }
@@ -407,11 +436,11 @@ int qvnt_reg_measure_mask_ex(qvnt_reg* reg, uint64_t mask, double u01, int renor
     uint64_t* d_idx = reinterpret_cast<uint64_t*>(reg->d_small);
     int* d_status = reinterpret_cast<int*>(reinterpret_cast<char*>(reg->d_small) + 8);
     QVNT_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), reg->stream));
-    TRY(launch_measure(reg->psi, reg->len, q_mask + 1, mask, u01, reg->scratch, d_idx, d_status, renormalise,
+    TRY(launch_measure(reg->psi, reg->fmt, reg->len, q_mask + 1, mask, u01, reg->scratch, d_idx, d_status, renormalise,
                        reg->stream));
     reg->launches += renormalise ? 9 : 6;
     QVNT_CUDA_TRY(cudaMemcpyAsync(reg->h_small, reg->d_small, 16, cudaMemcpyDeviceToHost, reg->stream));
-    QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
+    TRY(reg_sync(reg));
     uint64_t idx;
     int status;
     memcpy(&idx, reg->h_small, 8);
@@ -431,10 +460,10 @@ int qvnt_reg_get_absolute(qvnt_reg* reg, double* out) {
     if (!out) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
     double* d_abs = reinterpret_cast<double*>(reg->d_small) + 2;
-    TRY(launch_norm_sqr_sum(reg->psi, reg->len, reg->scratch, d_abs, reg->stream));
+    TRY(launch_norm_sqr_sum(reg->psi, reg->fmt, reg->len, reg->scratch, d_abs, reg->stream));
     reg->launches += 2;
     QVNT_CUDA_TRY(cudaMemcpyAsync(reg->h_small, d_abs, 8, cudaMemcpyDeviceToHost, reg->stream));
-    QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
+    TRY(reg_sync(reg));
     memcpy(out, reg->h_small, 8);
     return QVNT_OK;
 }
@@ -447,14 +476,15 @@ int qvnt_reg_get_probabilities(qvnt_reg* reg, double* host_out) {
     double* d_inv = d_abs + 1;
     int* d_status = reinterpret_cast<int*>(reinterpret_cast<char*>(reg->d_small) + 8);
     QVNT_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), reg->stream));
-    TRY(launch_norm_sqr_sum(reg->psi, reg->len, reg->scratch, d_abs, reg->stream));
+    TRY(launch_norm_sqr_sum(reg->psi, reg->fmt, reg->len, reg->scratch, d_abs, reg->stream));
     TRY(launch_inv(d_abs, d_inv, d_status, reg->stream));
     const uint64_t q_size = 1ull << reg->q_num;
     const uint64_t piece = q_size < (1ull << 23) ? q_size : (1ull << 23);
     TRY(reg_ensure_staging(reg, piece * sizeof(double)));
     for (uint64_t first = 0; first < q_size; first += piece) {
         const uint64_t n = (q_size - first) < piece ? (q_size - first) : piece;
-        TRY(launch_probabilities(reg->psi, first, n, d_inv, reinterpret_cast<double*>(reg->staging), reg->stream));
+        TRY(launch_probabilities(reg->psi, reg->fmt, first, n, d_inv, reinterpret_cast<double*>(reg->staging),
+                                 reg->stream));
         QVNT_CUDA_TRY(cudaMemcpyAsync(host_out + first, reg->staging, n * sizeof(double), cudaMemcpyDeviceToHost,
                                       reg->stream));
         QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
@@ -473,10 +503,31 @@ int qvnt_reg_get_polar(qvnt_reg* reg, double* host_out) {
     TRY(reg_ensure_staging(reg, piece * 2 * sizeof(double)));
     for (uint64_t first = 0; first < q_size; first += piece) {
         const uint64_t n = (q_size - first) < piece ? (q_size - first) : piece;
-        TRY(launch_polar(reg->psi, first, n, reinterpret_cast<double*>(reg->staging), reg->stream));
+        TRY(launch_polar(reg->psi, reg->fmt, first, n, reinterpret_cast<double*>(reg->staging), reg->stream));
         QVNT_CUDA_TRY(cudaMemcpyAsync(host_out + 2 * first, reg->staging, 2 * n * sizeof(double),
                                       cudaMemcpyDeviceToHost, reg->stream));
         QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
+        reg->launches += 1;
+    }
+    return QVNT_OK;
+}
+
+// Device -> host copy of amplitudes [first, first + count) as IEEE f64.  Double-float registers
+// are converted piecewise through the staging buffer; the state itself is not modified.
+static int copy_amplitudes_out(qvnt_reg* reg, uint64_t first, uint64_t count, double* host_out) {
+    if (reg->fmt == FMT_F64) {
+        QVNT_CUDA_TRY(cudaMemcpyAsync(host_out, reg->psi + first, count * sizeof(amp_t), cudaMemcpyDeviceToHost,
+                                      reg->stream));
+        return reg_sync(reg);
+    }
+    const uint64_t piece = count < (1ull << 22) ? count : (1ull << 22);
+    TRY(reg_ensure_staging(reg, piece * sizeof(amp_t)));
+    for (uint64_t at = 0; at < count; at += piece) {
+        const uint64_t n = (count - at) < piece ? (count - at) : piece;
+        TRY(launch_copy_out(reg->psi, reg->fmt, first + at, n, reinterpret_cast<double2*>(reg->staging), reg->stream));
+        QVNT_CUDA_TRY(cudaMemcpyAsync(host_out + 2 * at, reg->staging, n * sizeof(amp_t), cudaMemcpyDeviceToHost,
+                                      reg->stream));
+        TRY(reg_sync(reg));
         reg->launches += 1;
     }
     return QVNT_OK;
@@ -486,9 +537,7 @@ int qvnt_reg_get_amplitudes(qvnt_reg* reg, double* host_out) {
     CHECK_REG(reg);
     if (!host_out) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
-    QVNT_CUDA_TRY(cudaMemcpyAsync(host_out, reg->psi, reg->len * sizeof(amp_t), cudaMemcpyDeviceToHost, reg->stream));
-    QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
-    return QVNT_OK;
+    return copy_amplitudes_out(reg, 0, reg->len, host_out);
 }
 
 int qvnt_reg_get_amplitudes_range(qvnt_reg* reg, uint64_t first, uint64_t count, double* host_out) {
@@ -499,10 +548,7 @@ int qvnt_reg_get_amplitudes_range(qvnt_reg* reg, uint64_t first, uint64_t count,
                          (unsigned long long)count, (unsigned long long)reg->len);
     if (count == 0) return QVNT_OK;
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
-    QVNT_CUDA_TRY(cudaMemcpyAsync(host_out, reg->psi + first, count * sizeof(amp_t), cudaMemcpyDeviceToHost,
-                                  reg->stream));
-    QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
-    return QVNT_OK;
+    return copy_amplitudes_out(reg, first, count, host_out);
 }
 
 int qvnt_reg_set_amplitudes(qvnt_reg* reg, const double* host_in) {
@@ -510,15 +556,18 @@ int qvnt_reg_set_amplitudes(qvnt_reg* reg, const double* host_in) {
     if (!host_in) return set_error(QVNT_ERR_BAD_ARG, "null input pointer");
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
     QVNT_CUDA_TRY(cudaMemcpyAsync(reg->psi, host_in, reg->len * sizeof(amp_t), cudaMemcpyHostToDevice, reg->stream));
-    QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
-    return QVNT_OK;
+    if (reg->fmt == FMT_DF64) {
+        TRY(launch_convert(reg->psi, reg->len, 1, reg->stream));  // f64 -> double-float, in place
+        reg->launches += 1;
+    }
+    return reg_sync(reg);
 }
 
 int qvnt_reg_reset(qvnt_reg* reg, uint64_t state) {
     CHECK_REG(reg);
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
     const uint64_t q_mask = (1ull << reg->q_num) - 1;
-    TRY(launch_reset(reg->psi, reg->len, state & q_mask, reg->stream));  // quant.rs:202-205
+    TRY(launch_reset(reg->psi, reg->fmt, reg->len, state & q_mask, reg->stream));  // quant.rs:202-205
     reg->launches += 1;
     return QVNT_OK;
 }
@@ -527,8 +576,8 @@ int qvnt_reg_normalize(qvnt_reg* reg) {
     CHECK_REG(reg);
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
     double* d_abs = reinterpret_cast<double*>(reg->d_small) + 2;
-    TRY(launch_norm_sqr_sum(reg->psi, reg->len, reg->scratch, d_abs, reg->stream));
-    TRY(launch_normalize(reg->psi, reg->len, d_abs, reg->stream));
+    TRY(launch_norm_sqr_sum(reg->psi, reg->fmt, reg->len, reg->scratch, d_abs, reg->stream));
+    TRY(launch_normalize(reg->psi, reg->fmt, reg->len, d_abs, reg->stream));
     reg->launches += 3;
     return QVNT_OK;
 }
@@ -538,7 +587,7 @@ int qvnt_reg_reset_by_mask(qvnt_reg* reg, uint64_t mask) {
     const uint64_t q_mask = (1ull << reg->q_num) - 1;
     if ((mask & q_mask) == q_mask) return qvnt_reg_reset(reg, 0);  // quant.rs:208-210
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
-    TRY(launch_zero_mask(reg->psi, reg->len, mask, reg->stream));
+    TRY(launch_zero_mask(reg->psi, reg->fmt, reg->len, mask, reg->stream));
     reg->launches += 1;
     return qvnt_reg_normalize(reg);
 }
@@ -556,7 +605,8 @@ int qvnt_reg_tensor(const qvnt_reg* a, const qvnt_reg* b, qvnt_reg** out) {
     qvnt_reg* r = nullptr;
     TRY(make_reg(a->ctx, q_num, &r));
     r->engine = a->engine;
-    int st = launch_tensor(a->psi, a->q_num, b->psi, b->q_num, r->psi, r->len, r->stream);
+    r->fmt = a->fmt;
+    int st = launch_tensor(a->psi, a->fmt, a->q_num, b->psi, b->fmt, b->q_num, r->psi, r->fmt, r->len, r->stream);
     if (st) {
         reg_free(r);
         return st;
@@ -592,11 +642,15 @@ int qvnt_apply_host(qvnt_ctx* ctx, const qvnt_gate* gates, size_t count, const d
         if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
     }
     QVNT_CUDA_TRY(cudaSetDevice(ctx->device));
+    // The plugin register is scratch: its storage is converted in place around the gate passes.
     QVNT_CUDA_TRY(cudaMemcpyAsync(r->psi, psi_i, len * sizeof(amp_t), cudaMemcpyHostToDevice, r->stream));
+    if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 1, r->stream));
     TRY(r->engine == QVNT_ENGINE_PLAIN ? apply_plain(r, gates, count) : apply_fused(r, gates, count));
+    if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 0, r->stream));
     QVNT_CUDA_TRY(cudaMemcpyAsync(psi_o, r->psi, len * sizeof(amp_t), cudaMemcpyDeviceToHost, r->stream));
-    QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));
-    return QVNT_OK;
+    if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 1, r->stream));
+    r->launches += r->fmt == FMT_DF64 ? 3 : 0;
+    return reg_sync(r);
 }
 
 int qvnt_reg_get_stream(const qvnt_reg* reg, void** stream) {

@@ -48,6 +48,7 @@ struct qvnt_reg {
     void* h_small = nullptr;     // pinned 64 B host mirror
     cudaStream_t stream = nullptr;
     int engine = QVNT_ENGINE_FUSED;
+    int fmt = 0;  // storage format (kernels.h Fmt): follows the engine
     uint32_t fusion_k = 0;
     uint64_t launches = 0;
     uint64_t passes = 0;
@@ -63,6 +64,7 @@ uint64_t gate_acts_on(const qvnt_gate& g);
 int gate_check_masks(const qvnt_gate& g);
 DevGate decode_gate(const qvnt_gate& g);
 int reg_ensure_alt(qvnt_reg* r);
+int reg_sync(qvnt_reg* r);
 int timing_begin(qvnt_reg* r, cudaEvent_t* stop);
 int timing_end(qvnt_reg* r, cudaEvent_t stop);
 int apply_plain(qvnt_reg* r, const qvnt_gate* gates, size_t count);

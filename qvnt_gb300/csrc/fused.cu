@@ -1,19 +1,26 @@
-// Fused engine: runs of gates applied to shared-memory tiles, one HBM round trip per pass.
+// Fused engine: runs of gates applied to shared-memory tiles, one HBM round trip per pass, in
+// double-float arithmetic (df64.cuh) on the FP32 pipes.
 //
 // qvnt applies every SingleOp as a full sweep over the state (src/operator/multi/mod.rs:97-114).
-// Here a host planner groups consecutive gates into PASSES.  A pass picks a set Q of k tile qubits
-// (always containing the lowest qubits, so each tile is read as contiguous runs); a tile is the
-// 2^k amplitudes that share all non-Q index bits.  Every CTA loads a tile into shared memory,
-// applies the pass's gates there, and writes it back once.  A gate joins a pass when its target
-// qubits lie in Q; its controls may lie anywhere (a control outside Q is a per-tile predicate),
-// and diagonal gates (Z, S, T, RZ, RZZ) join any pass, their phase taking the non-Q index bits
-// from the tile base.  Gates may move ahead of deferred gates only when both are diagonal or their
-// qubit supports are disjoint, so the result equals the in-order product up to rounding.
+// Here the host plans PASSES.  A pass picks k = 12 tile qubits Q, always containing the five lowest
+// qubits, so a tile -- the 2^12 amplitudes that share all non-Q index bits -- is 2^(12-5) contiguous
+// 512-byte runs.  Each CTA (256 threads, persistent over tiles):
+//   1. stages the tile into shared memory with TMA bulk copies (cp.async.bulk, one per run) that
+//      complete on an mbarrier;
+//   2. runs the pass's STAGES: a stage gives every thread 16 amplitudes in registers, spanning 4
+//      "register qubits" of the tile, applies every gate of the stage there, and writes back;
+//   3. writes the tile back with TMA bulk stores.
+// A gate joins a pass when its target qubits lie in Q; controls may lie anywhere (outside Q they
+// are a per-tile predicate, on thread bits a per-thread predicate) and diagonal gates (Z, S, T, RZ,
+// RZZ) join any pass and any stage.  A gate may overtake a deferred gate only when both are diagonal
+// or their qubit supports are disjoint, so the result is the in-order product up to rounding.
+// The pass descriptor (stages, gates, coefficients) is a __grid_constant__ kernel parameter.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
-#include "atomic.cuh"
+#include "df64.cuh"
 #include "engine.h"
 #include "kernels.h"
 
@@ -21,204 +28,684 @@ namespace qvnt {
 
 namespace {
 
-constexpr int kFusedThreads = 512;
-constexpr uint32_t kDefaultK = 12;
-constexpr size_t kLookahead = 4096;
+constexpr int kTileQ = 12;                         // qubits per tile
+constexpr int kRegQ = 4;                           // register qubits per thread
+constexpr int kSlots = 1 << kRegQ;                 // amplitudes per thread
+constexpr int kMaxThreads = 1 << (kTileQ - kRegQ);  // 256
+constexpr int kLowQ = 5;                           // lowest qubits always in a tile (512-byte runs)
+constexpr int kMaxGates = 192;
+constexpr int kMaxStages = 96;
+constexpr int kMaxCoef = 4096;
+constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier waits (iterations of try_wait)
 
-struct LGate {
-    DevGate g;        // masks in virtual-local coordinates (tile bit j = local bit j)
-    Enum e;           // orbit enumeration inside the tile
-    uint64_t gctrl;   // control bits outside the tile: gate applies where base & gctrl == gctrl
-    uint64_t a_nl;    // diagonal gates: bits of a outside the tile
-    uint64_t pmask;   // pair partner mask (shape 2)
-    uint32_t shape;   // 1 diagonal, 2 pair, 4 quad
-    uint32_t pad;
+enum : uint8_t { OP_G1 = 1, OP_G2P = 2, OP_G4 = 3, OP_DIAG = 4 };
+enum : uint8_t { F_ID = 0, F_PERM = 1, F_RX = 2, F_REAL = 3, F_GEN = 4 };
+enum : uint8_t { D_PAR = 0, D_POP = 1 };
+
+struct DGate {
+    uint64_t ctrl_out;  // control bits outside the tile (global mask)
+    uint64_t dm_out;    // diagonal mask bits outside the tile (global mask)
+    uint32_t coef;      // offset into the coefficient pool (floats)
+    uint32_t codes;     // exact phase codes: F_PERM (c01 | c10 << 4); diagonal tables (4 bits per entry)
+    uint16_t ctrl_thr;  // controls on thread bits (thread-index mask)
+    uint16_t dm_thr;    // diagonal mask on thread bits
+    uint8_t ctrl_reg;   // controls on register bits (slot mask)
+    uint8_t dm_reg;     // diagonal mask on register bits
+    uint8_t op, form0, form1, b0, b1, dkind;
+    uint8_t exact;      // diagonal: every table entry is a power of i
+    uint8_t pad[7];
 };
+static_assert(sizeof(DGate) == 48, "DGate layout");
 
-struct TileGeom {
-    uint32_t k;         // tile qubits
-    uint32_t c;         // length of the contiguous low run (tile qubits 0..c-1 are qubits 0..c-1)
-    uint32_t nhigh;     // k - c
-    uint32_t pad;
-    uint32_t high[kFusedMaxK];  // global positions of tile bits c..k-1
-    uint32_t qpos[kFusedMaxK];  // global positions of all k tile bits
-    Enum tiles;         // tile t -> base index (tile qubits inserted as 0)
+struct DStage {
+    uint8_t rbit[kRegQ];   // tile-local bit of register bit b
+    uint8_t tbit[kTileQ - kRegQ];  // tile-local bit of thread bit i
+    uint16_t gbegin, gend;
 };
+static_assert(sizeof(DStage) == 16, "DStage layout");
 
-__device__ __forceinline__ void apply_local(amp_t* __restrict__ tile, const LGate& G, uint64_t extra) {
-    const uint64_t count = G.e.count;
-    if (G.shape == 1) {
-        for (uint64_t j = threadIdx.x; j < count; j += kFusedThreads) {
-            const uint64_t l = enum_index(G.e, j);
-            const amp_t x = tile[l];
-            tile[l] = atomic_op(G.g, l | extra, [&](uint64_t) { return x; });
-        }
-    } else if (G.shape == 2) {
-        const uint64_t pm = G.pmask;
-        for (uint64_t j = threadIdx.x; j < count; j += kFusedThreads) {
-            const uint64_t l0 = enum_index(G.e, j), l1 = l0 ^ pm;
-            const amp_t x0 = tile[l0], x1 = tile[l1];
-            auto f = [&](uint64_t q) { return q == l0 ? x0 : x1; };
-            const amp_t o0 = atomic_op(G.g, l0, f);
-            const amp_t o1 = atomic_op(G.g, l1, f);
-            tile[l0] = o0;
-            tile[l1] = o1;
-        }
-    } else {
-        const uint64_t a = G.g.a, b = G.g.b;
-        for (uint64_t j = threadIdx.x; j < count; j += kFusedThreads) {
-            const uint64_t l0 = enum_index(G.e, j);
-            const amp_t x0 = tile[l0], x1 = tile[l0 | a], x2 = tile[l0 | b], x3 = tile[l0 | a | b];
-            auto f = [&](uint64_t q) {
-                const int s = ((q & a) ? 1 : 0) | ((q & b) ? 2 : 0);
-                return s == 0 ? x0 : (s == 1 ? x1 : (s == 2 ? x2 : x3));
-            };
-            const amp_t o0 = atomic_op(G.g, l0, f);
-            const amp_t o1 = atomic_op(G.g, l0 | a, f);
-            const amp_t o2 = atomic_op(G.g, l0 | b, f);
-            const amp_t o3 = atomic_op(G.g, l0 | a | b, f);
-            tile[l0] = o0;
-            tile[l0 | a] = o1;
-            tile[l0 | b] = o2;
-            tile[l0 | a | b] = o3;
+struct PassParams {
+    uint64_t ntiles;
+    uint32_t k;        // tile qubits of this pass (<= 12)
+    uint32_t c;        // contiguous low run: tile-local bits 0..c-1 are qubits 0..c-1
+    uint32_t nthreads;  // 2^(k - 4)
+    uint32_t nstages;
+    uint32_t tq[kTileQ];   // global qubit of tile-local bit p (ascending)
+    DStage stages[kMaxStages];
+    DGate gates[kMaxGates];
+    float coef[kMaxCoef];
+};
+static_assert(sizeof(PassParams) <= 32760, "pass descriptor must fit the kernel-parameter space");
+
+// ---- TMA / mbarrier helpers (inline PTX) ------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void tma_load_1d(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(smem_dst)),
+                 "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tma_store_1d(void* gdst, const void* smem_src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(smem_u32(smem_src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// ---- register-level gate application ------------------------------------------------------------
+__device__ __forceinline__ df cdf(const PassParams& P, uint32_t o) { return df{P.coef[o], P.coef[o + 1]}; }
+
+// One 2x2 block on the pair (x0, x1): [y0; y1] = M [x0; x1].
+template <int FORM>
+__device__ __forceinline__ void pair_op(dfc& x0, dfc& x1, const PassParams& P, uint32_t o, uint32_t codes) {
+    if (FORM == F_PERM) {
+        const dfc n0 = dfc_rotate(x1, codes & 3u);
+        const dfc n1 = dfc_rotate(x0, (codes >> 4) & 3u);
+        x0 = n0;
+        x1 = n1;
+    } else if (FORM == F_RX) {
+        // [[a, i b], [i c, d]] with a, b, c, d real
+        const df a = cdf(P, o), b = cdf(P, o + 2), c = cdf(P, o + 4), d = cdf(P, o + 6);
+        dfc n0, n1;
+        n0.re = df_lin2(a, x0.re, df_neg(b), x1.im);
+        n0.im = df_lin2(a, x0.im, b, x1.re);
+        n1.re = df_lin2(df_neg(c), x0.im, d, x1.re);
+        n1.im = df_lin2(c, x0.re, d, x1.im);
+        x0 = n0;
+        x1 = n1;
+    } else if (FORM == F_REAL) {
+        const df a = cdf(P, o), b = cdf(P, o + 2), c = cdf(P, o + 4), d = cdf(P, o + 6);
+        dfc n0, n1;
+        n0.re = df_lin2(a, x0.re, b, x1.re);
+        n0.im = df_lin2(a, x0.im, b, x1.im);
+        n1.re = df_lin2(c, x0.re, d, x1.re);
+        n1.im = df_lin2(c, x0.im, d, x1.im);
+        x0 = n0;
+        x1 = n1;
+    } else if (FORM == F_GEN) {
+        const df ar = cdf(P, o), ai = cdf(P, o + 2), br = cdf(P, o + 4), bi = cdf(P, o + 6);
+        const df cr = cdf(P, o + 8), ci = cdf(P, o + 10), dr = cdf(P, o + 12), di = cdf(P, o + 14);
+        dfc n0, n1;
+        n0.re = df_lin4(ar, x0.re, df_neg(ai), x0.im, br, x1.re, df_neg(bi), x1.im);
+        n0.im = df_lin4(ar, x0.im, ai, x0.re, br, x1.im, bi, x1.re);
+        n1.re = df_lin4(cr, x0.re, df_neg(ci), x0.im, dr, x1.re, df_neg(di), x1.im);
+        n1.im = df_lin4(cr, x0.im, ci, x0.re, dr, x1.im, di, x1.re);
+        x0 = n0;
+        x1 = n1;
+    }
+}
+
+template <int B, int FORM>
+__device__ __forceinline__ void g1_form(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
+    const uint32_t creg = G.ctrl_reg;
+#pragma unroll
+    for (int j = 0; j < kSlots; ++j) {
+        if (j & (1 << B)) continue;
+        if (tok && (j & creg) == creg) pair_op<FORM>(v[j], v[j | (1 << B)], P, G.coef, G.codes);
+    }
+}
+
+template <int B>
+__device__ __forceinline__ void g1(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
+    switch (G.form0) {
+    case F_PERM: g1_form<B, F_PERM>(v, P, G, tok); break;
+    case F_RX: g1_form<B, F_RX>(v, P, G, tok); break;
+    case F_REAL: g1_form<B, F_REAL>(v, P, G, tok); break;
+    default: g1_form<B, F_GEN>(v, P, G, tok); break;
+    }
+}
+
+// Two-qubit gate as 2x2 blocks on the pairs (00, 11) [block A] and (01, 10) [block B] of register
+// bits B0 < B1; member order inside a pair: the one with bit B0 clear in A, set in B, first.
+template <int B0, int B1, int FORM>
+__device__ __forceinline__ void g2p_block(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok,
+                                          bool blockA, uint32_t o, uint32_t codes) {
+    constexpr int M0 = 1 << B0, M1 = 1 << B1;
+    const uint32_t creg = G.ctrl_reg;
+#pragma unroll
+    for (int j = 0; j < kSlots; ++j) {
+        if (j & (M0 | M1)) continue;
+        if (!(tok && (j & creg) == creg)) continue;
+        if (blockA)
+            pair_op<FORM>(v[j], v[j | M0 | M1], P, o, codes);
+        else
+            pair_op<FORM>(v[j | M0], v[j | M1], P, o, codes);
+    }
+}
+
+template <int B0, int B1>
+__device__ __forceinline__ void g2p_any(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok, bool blockA) {
+    const uint8_t form = blockA ? G.form0 : G.form1;
+    const uint32_t o = G.coef + (blockA ? 0u : 16u);
+    const uint32_t codes = blockA ? (G.codes & 0xffu) : ((G.codes >> 8) & 0xffu);
+    switch (form) {
+    case F_ID: break;
+    case F_PERM: g2p_block<B0, B1, F_PERM>(v, P, G, tok, blockA, o, codes); break;
+    case F_RX: g2p_block<B0, B1, F_RX>(v, P, G, tok, blockA, o, codes); break;
+    case F_REAL: g2p_block<B0, B1, F_REAL>(v, P, G, tok, blockA, o, codes); break;
+    default: g2p_block<B0, B1, F_GEN>(v, P, G, tok, blockA, o, codes); break;
+    }
+}
+
+template <int B0, int B1>
+__device__ __forceinline__ void g2p(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
+    g2p_any<B0, B1>(v, P, G, tok, true);
+    g2p_any<B0, B1>(v, P, G, tok, false);
+}
+
+// Dense 4x4 on register bits B0 < B1; member r = (bit B0) | (bit B1) << 1, row-major complex matrix.
+template <int B0, int B1>
+__device__ __forceinline__ void g4(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
+    constexpr int M0 = 1 << B0, M1 = 1 << B1;
+    const uint32_t creg = G.ctrl_reg;
+    const uint32_t o = G.coef;
+#pragma unroll
+    for (int j = 0; j < kSlots; ++j) {
+        if (j & (M0 | M1)) continue;
+        if (!(tok && (j & creg) == creg)) continue;
+        const int s[4] = {j, j | M0, j | M1, j | M0 | M1};
+        dfc x[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) x[c] = v[s[c]];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            df tr[8], ti[8];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const df mr = cdf(P, o + 16 * r + 4 * c), mi = cdf(P, o + 16 * r + 4 * c + 2);
+                tr[2 * c] = df_mul_raw(mr, x[c].re);
+                tr[2 * c + 1] = df_mul_raw(df_neg(mi), x[c].im);
+                ti[2 * c] = df_mul_raw(mr, x[c].im);
+                ti[2 * c + 1] = df_mul_raw(mi, x[c].re);
+            }
+            v[s[r]].re = df_sum<8>(tr);
+            v[s[r]].im = df_sum<8>(ti);
         }
     }
 }
 
-__global__ void __launch_bounds__(kFusedThreads) fused_pass_kernel(amp_t* __restrict__ psi,
-                                                                   const LGate* __restrict__ gates,
-                                                                   uint32_t ngates, const TileGeom tg) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    amp_t* tile = reinterpret_cast<amp_t*>(smem_raw);
-    const uint32_t T = 1u << tg.k;
-    uint64_t* seg = reinterpret_cast<uint64_t*>(tile + T);
-    const uint32_t nseg = 1u << tg.nhigh;
-    const uint32_t cmask = (1u << tg.c) - 1u;
-    for (uint32_t s = threadIdx.x; s < nseg; s += kFusedThreads) {
+__device__ __forceinline__ void gdiag(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok, uint32_t tid,
+                                      uint64_t base) {
+    if (!tok) return;
+    const uint32_t cnt0 = __popc(tid & G.dm_thr) + __popcll(base & G.dm_out);
+    const uint32_t creg = G.ctrl_reg, dreg = G.dm_reg;
+    if (G.exact) {
+        const uint32_t codes = G.codes;
+        const uint32_t idxmask = G.dkind == D_PAR ? 1u : 7u;
+#pragma unroll
+        for (int j = 0; j < kSlots; ++j) {
+            if ((j & creg) != creg) continue;
+            const uint32_t k = (cnt0 + __popc(j & dreg)) & idxmask;
+            v[j] = dfc_rotate(v[j], (codes >> (4 * k)) & 3u);
+        }
+    } else if (G.dkind == D_PAR) {
+        const uint32_t o = G.coef;
+        const df r0 = cdf(P, o), i0 = cdf(P, o + 2), r1 = cdf(P, o + 4), i1 = cdf(P, o + 6);
+#pragma unroll
+        for (int j = 0; j < kSlots; ++j) {
+            if ((j & creg) != creg) continue;
+            const bool odd = (cnt0 + __popc(j & dreg)) & 1u;
+            v[j] = dfc_mul(odd ? r1 : r0, odd ? i1 : i0, v[j]);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kSlots; ++j) {
+            if ((j & creg) != creg) continue;
+            const uint32_t o = G.coef + 4u * ((cnt0 + __popc(j & dreg)) & 7u);
+            v[j] = dfc_mul(cdf(P, o), cdf(P, o + 2), v[j]);
+        }
+    }
+}
+
+__device__ __forceinline__ void apply_gate(dfc (&v)[kSlots], const PassParams& P, const DGate& G, uint32_t tid,
+                                           uint64_t base) {
+    if ((base & G.ctrl_out) != G.ctrl_out) return;
+    const bool tok = (tid & G.ctrl_thr) == G.ctrl_thr;
+    switch (G.op) {
+    case OP_G1:
+        switch (G.b0) {
+        case 0: g1<0>(v, P, G, tok); break;
+        case 1: g1<1>(v, P, G, tok); break;
+        case 2: g1<2>(v, P, G, tok); break;
+        default: g1<3>(v, P, G, tok); break;
+        }
+        break;
+    case OP_G2P:
+    case OP_G4: {
+        const int pr = G.b0 * 4 + G.b1;
+        const bool d = G.op == OP_G4;
+        switch (pr) {
+        case 1: d ? g4<0, 1>(v, P, G, tok) : g2p<0, 1>(v, P, G, tok); break;
+        case 2: d ? g4<0, 2>(v, P, G, tok) : g2p<0, 2>(v, P, G, tok); break;
+        case 3: d ? g4<0, 3>(v, P, G, tok) : g2p<0, 3>(v, P, G, tok); break;
+        case 6: d ? g4<1, 2>(v, P, G, tok) : g2p<1, 2>(v, P, G, tok); break;
+        case 7: d ? g4<1, 3>(v, P, G, tok) : g2p<1, 3>(v, P, G, tok); break;
+        default: d ? g4<2, 3>(v, P, G, tok) : g2p<2, 3>(v, P, G, tok); break;
+        }
+        break;
+    }
+    default:
+        gdiag(v, P, G, tok, tid, base);
+        break;
+    }
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 2)
+    fused_df_kernel(float4* __restrict__ psi, const __grid_constant__ PassParams P, int* __restrict__ err) {
+    extern __shared__ __align__(128) float4 tile[];
+    __shared__ uint64_t seg_off[1 << (kTileQ - kLowQ)];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ int s_abort;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t nthr = P.nthreads;
+    const uint32_t nseg = 1u << (P.k - P.c);
+    const uint32_t seg_amps = 1u << P.c;
+    for (uint32_t s = tid; s < nseg; s += nthr) {
         uint64_t off = 0;
-        for (uint32_t j = 0; j < tg.nhigh; ++j)
-            if ((s >> j) & 1u) off |= 1ull << tg.high[j];
-        seg[s] = off;
+        for (uint32_t j = 0; j < P.k - P.c; ++j)
+            if ((s >> j) & 1u) off |= 1ull << P.tq[P.c + j];
+        seg_off[s] = off;
+    }
+    if (tid == 0) {
+        mbar_init(&mbar, 1);
+        fence_mbar_init();
+        s_abort = 0;
     }
     __syncthreads();
-    for (uint64_t t = blockIdx.x; t < tg.tiles.count; t += gridDim.x) {
-        const uint64_t base = enum_index(tg.tiles, t);
-        for (uint32_t l = threadIdx.x; l < T; l += kFusedThreads)
-            tile[l] = psi[base | seg[l >> tg.c] | (l & cmask)];
+    uint32_t phase = 0;
+    for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
+        // tile base: tile index with zeros inserted at the tile qubits
+        uint64_t base = t;
+        for (uint32_t p = 0; p < P.k; ++p) {
+            const uint32_t q = P.tq[p];
+            base = ((base >> q) << (q + 1)) | (base & ((1ull << q) - 1ull));
+        }
+        if (tid < 32) {
+            if (tid == 0) {
+                fence_proxy_async();
+                mbar_arrive_expect_tx(&mbar, (1u << P.k) * 16u);
+            }
+            __syncwarp(nthr >= 32 ? 0xffffffffu : ((1u << nthr) - 1u));
+            for (uint32_t s = tid; s < nseg; s += 32)
+                tma_load_1d(tile + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 16u, &mbar);
+        }
+        uint32_t it = 0;
+        while (!mbar_try_wait(&mbar, phase)) {
+            if (++it >= kWaitLimit) {
+                atomicExch(err, 1);
+                s_abort = 1;
+                break;
+            }
+        }
+        phase ^= 1u;
         __syncthreads();
-        for (uint32_t gi = 0; gi < ngates; ++gi) {
-            const LGate& G = gates[gi];
-            if ((base & G.gctrl) != G.gctrl) continue;
-            const uint64_t extra = G.a_nl ? (((1ull << __popcll(base & G.a_nl)) - 1ull) << tg.k) : 0ull;
-            apply_local(tile, G, extra);
+        if (s_abort) {
+            // the copies may still land: wait for them (bounded) before leaving
+            uint32_t it2 = 0;
+            while (!mbar_try_wait(&mbar, phase ^ 1u) && ++it2 < kWaitLimit) {
+            }
+            return;
+        }
+        for (uint32_t si = 0; si < P.nstages; ++si) {
+            const DStage& S = P.stages[si];
+            uint32_t tl = 0;
+#pragma unroll
+            for (int i = 0; i < kTileQ - kRegQ; ++i)
+                if (i < (int)(P.k - kRegQ) && ((tid >> i) & 1u)) tl |= 1u << S.tbit[i];
+            uint32_t roff[kRegQ];
+#pragma unroll
+            for (int b = 0; b < kRegQ; ++b) roff[b] = 1u << S.rbit[b];
+            dfc v[kSlots];
+#pragma unroll
+            for (int j = 0; j < kSlots; ++j) {
+                uint32_t l = tl;
+#pragma unroll
+                for (int b = 0; b < kRegQ; ++b)
+                    if (j & (1 << b)) l += roff[b];
+                const float4 a = tile[l];
+                v[j].re = df{a.x, a.y};
+                v[j].im = df{a.z, a.w};
+            }
+            for (uint32_t gi = S.gbegin; gi < S.gend; ++gi) apply_gate(v, P, P.gates[gi], tid, base);
+#pragma unroll
+            for (int j = 0; j < kSlots; ++j) {
+                uint32_t l = tl;
+#pragma unroll
+                for (int b = 0; b < kRegQ; ++b)
+                    if (j & (1 << b)) l += roff[b];
+                tile[l] = make_float4(v[j].re.h, v[j].re.l, v[j].im.h, v[j].im.l);
+            }
             __syncthreads();
         }
-        for (uint32_t l = threadIdx.x; l < T; l += kFusedThreads)
-            psi[base | seg[l >> tg.c] | (l & cmask)] = tile[l];
+        fence_proxy_async();
+        __syncthreads();
+        if (tid < 32) {
+            for (uint32_t s = tid; s < nseg; s += 32)
+                tma_store_1d(psi + (base | seg_off[s]), tile + (size_t)s * seg_amps, seg_amps * 16u);
+            bulk_commit();
+            bulk_wait_read0();
+        }
         __syncthreads();
     }
+    if (tid < 32) bulk_wait0();
+}
+
+// ---- host: lowering qvnt gates to engine gates ----------------------------------------------------
+struct C2 {
+    double re, im;
+};
+
+struct EGate {
+    uint8_t op = 0;
+    uint8_t form0 = F_ID, form1 = F_ID;
+    uint8_t dkind = D_PAR;
+    bool exact = false;
+    int q0 = -1, q1 = -1;   // target qubits (q0 < q1 for two-qubit ops)
+    uint64_t ctrl = 0;
+    uint64_t dmask = 0;
+    uint32_t codes = 0;
+    std::vector<float> coef;  // df64 pairs
+    int cost = 0;             // FP32 instructions per amplitude (estimate)
+    bool standalone = false;
+    size_t src = 0;
+};
+
+void push_df(std::vector<float>& out, double x) {
+    const float h = (float)x;
+    out.push_back(h);
+    out.push_back((float)(x - (double)h));
 }
 
 inline unsigned popc(uint64_t x) { return (unsigned)__builtin_popcountll(x); }
 
-bool is_diag(uint32_t kind) {
-    return kind == QVNT_GATE_Z || kind == QVNT_GATE_S || kind == QVNT_GATE_T || kind == QVNT_GATE_RZ ||
-           kind == QVNT_GATE_RZZ;
+// i^code for the exact phases.
+int exact_code(C2 z) {
+    if (z.re == 1.0 && z.im == 0.0) return 0;
+    if (z.re == 0.0 && z.im == 1.0) return 1;
+    if (z.re == -1.0 && z.im == 0.0) return 2;
+    if (z.re == 0.0 && z.im == -1.0) return 3;
+    return -1;
 }
 
-struct GInfo {
-    uint64_t targets = 0;
-    uint64_t touched = 0;
-    bool diag = false;
-    bool skip = false;
-    bool standalone = false;
-};
-
-GInfo classify(const qvnt_gate& g, uint32_t k, uint32_t c) {
-    GInfo r;
-    const DevGate d = decode_gate(g);
-    if (plain_gate_is_identity(d)) {
-        r.skip = true;
-        return r;
+int form_cost(uint8_t f) {
+    switch (f) {
+    case F_ID: return 0;
+    case F_PERM: return 4;
+    case F_RX: case F_REAL: return 40;
+    default: return 85;
     }
-    r.diag = is_diag(g.kind);
-    if (!r.diag) r.targets = (g.kind == QVNT_GATE_H2 || g.kind == QVNT_GATE_U2) ? (g.a_mask | g.b_mask) : g.a_mask;
-    r.touched = r.targets | g.ctrl | (r.diag ? g.a_mask : 0);
-    if (plain_gate_needs_gather(d)) r.standalone = true;
-    const uint64_t low = (1ull << c) - 1ull;
-    if (popc(r.targets & ~low) > k - c) r.standalone = true;
-    return r;
 }
 
-// Maps global index bits to tile-local positions through `qpos`.
-uint64_t compress(uint64_t m, const uint32_t* qpos, uint32_t k) {
-    uint64_t r = 0;
-    for (uint32_t j = 0; j < k; ++j)
-        if ((m >> qpos[j]) & 1ull) r |= 1ull << j;
-    return r;
-}
-
-Enum local_enum(uint32_t k, uint64_t inserted, uint64_t ones) {
-    Enum e{};
-    uint32_t n = 0;
-    for (uint32_t p = 0; p < k; ++p)
-        if ((inserted >> p) & 1ull) e.ins[n++] = p;
-    e.nins = n;
-    e.ones = ones;
-    e.count = (1ull << k) >> n;
+EGate diag_gate(uint64_t mask, uint64_t ctrl, const std::vector<C2>& table, uint8_t dkind) {
+    EGate e;
+    e.op = OP_DIAG;
+    e.dmask = mask;
+    e.ctrl = ctrl;
+    e.dkind = dkind;
+    bool exact = true;
+    uint32_t codes = 0;
+    for (size_t k = 0; k < table.size(); ++k) {
+        const int c = exact_code(table[k]);
+        if (c < 0) exact = false;
+        else codes |= (uint32_t)c << (4 * k);
+    }
+    e.exact = exact;
+    e.codes = codes;
+    if (!exact)
+        for (const C2& z : table) {
+            push_df(e.coef, z.re);
+            push_df(e.coef, z.im);
+        }
+    e.cost = exact ? 8 : 42;
     return e;
 }
 
-LGate lower_gate(const qvnt_gate& g, const uint32_t* qpos, uint32_t k, uint64_t qmask) {
-    LGate L;
-    memset(&L, 0, sizeof L);
-    DevGate d = decode_gate(g);
-    const uint64_t ctrl_l = compress(g.ctrl & qmask, qpos, k);
-    L.gctrl = g.ctrl & ~qmask;
-    d.ctrl = ctrl_l;
-    if (is_diag(g.kind)) {
-        const uint64_t a_l = compress(g.a_mask & qmask, qpos, k);
-        L.a_nl = g.a_mask & ~qmask;
-        // Non-tile bits of a become popcount(a_nl) virtual bits above the tile (set per tile).
-        d.a = a_l | (((1ull << popc(L.a_nl)) - 1ull) << k);
-        L.shape = 1;
-        L.e = local_enum(k, ctrl_l, ctrl_l);
-    } else {
-        d.a = compress(g.a_mask, qpos, k);
-        d.b = compress(d.b, qpos, k);
-        switch (g.kind) {
-        case QVNT_GATE_SWAP: case QVNT_GATE_ISWAP: case QVNT_GATE_SQRT_SWAP: case QVNT_GATE_SQRT_ISWAP: {
-            const uint64_t lo = d.a & (~d.a + 1ull);
-            L.shape = 2;
-            L.pmask = d.a;
-            L.e = local_enum(k, ctrl_l | d.a, ctrl_l | lo);
-            break;
-        }
-        case QVNT_GATE_H2: case QVNT_GATE_U2:
-            L.shape = 4;
-            L.e = local_enum(k, ctrl_l | d.a | d.b, ctrl_l);
-            break;
-        default: {
-            const uint64_t pivot = 1ull << (63 - __builtin_clzll(d.a));
-            L.shape = 2;
-            L.pmask = d.a;
-            L.e = local_enum(k, ctrl_l | pivot, ctrl_l);
-            break;
-        }
-        }
-    }
-    L.g = d;
-    return L;
+EGate g1_gate(int q, uint64_t ctrl, uint8_t form, double a, double b, double c, double d) {
+    EGate e;
+    e.op = OP_G1;
+    e.q0 = q;
+    e.ctrl = ctrl;
+    e.form0 = form;
+    push_df(e.coef, a);
+    push_df(e.coef, b);
+    push_df(e.coef, c);
+    push_df(e.coef, d);
+    e.cost = form_cost(form);
+    return e;
 }
 
-struct Pass {
+EGate g1_perm(int q, uint64_t ctrl, int c01, int c10) {
+    EGate e;
+    e.op = OP_G1;
+    e.q0 = q;
+    e.ctrl = ctrl;
+    e.form0 = F_PERM;
+    e.codes = (uint32_t)c01 | ((uint32_t)c10 << 4);
+    e.cost = 4;
+    return e;
+}
+
+void push_block(EGate& e, uint8_t form, const C2* m) {  // m: row-major 2x2
+    if (form == F_RX || form == F_REAL) {
+        const double a = m[0].re, d = m[3].re;
+        const double b = form == F_RX ? m[1].im : m[1].re, c = form == F_RX ? m[2].im : m[2].re;
+        push_df(e.coef, a);
+        push_df(e.coef, b);
+        push_df(e.coef, c);
+        push_df(e.coef, d);
+        for (int k = 0; k < 8; ++k) e.coef.push_back(0.f);  // blocks are 16 floats apart
+    } else {
+        for (int k = 0; k < 4; ++k) {
+            push_df(e.coef, m[k].re);
+            push_df(e.coef, m[k].im);
+        }
+    }
+}
+
+// Two-qubit gate as blocks on (00, 11) and (01, 10).
+EGate g2p_gate(uint64_t ab, uint64_t ctrl, uint8_t fa, const C2* ma, uint32_t codes_a, uint8_t fb, const C2* mb,
+               uint32_t codes_b) {
+    EGate e;
+    e.op = OP_G2P;
+    e.q0 = __builtin_ctzll(ab);
+    e.q1 = 63 - __builtin_clzll(ab);
+    e.ctrl = ctrl;
+    e.form0 = fa;
+    e.form1 = fb;
+    e.codes = codes_a | (codes_b << 8);
+    const C2 zero[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    push_block(e, fa == F_PERM || fa == F_ID ? F_GEN : fa, fa == F_PERM || fa == F_ID ? zero : ma);
+    push_block(e, fb == F_PERM || fb == F_ID ? F_GEN : fb, fb == F_PERM || fb == F_ID ? zero : mb);
+    e.cost = (form_cost(fa) + form_cost(fb) + 1) / 2 + 2;
+    return e;
+}
+
+// Lowers one validated qvnt gate (the atomic formulas of src/operator/atomic/*.rs written as the
+// matrices they apply) to engine gates.
+void lower(const qvnt_gate& g, size_t src, std::vector<EGate>& out) {
+    const uint64_t a = g.a_mask, ctrl = g.ctrl;
+    const double c = g.phase[0], s = g.phase[1];
+    const double r = 0.70710678118654752440084436210484903;
+    auto each_bit = [&](uint64_t m, auto&& f) {
+        for (int q = 0; q < 64; ++q)
+            if ((m >> q) & 1ull) f(q);
+    };
+    switch (g.kind) {
+    case QVNT_GATE_ID:
+        return;
+    case QVNT_GATE_X:  // x.rs: a product of single-bit flips (exact)
+        each_bit(a, [&](int q) { out.push_back(g1_perm(q, ctrl, 0, 0)); });
+        return;
+    case QVNT_GATE_Y:  // y.rs: Y(mask) = tensor product of single-qubit Y = [[0, -i], [i, 0]] (exact)
+        each_bit(a, [&](int q) { out.push_back(g1_perm(q, ctrl, 3, 1)); });
+        return;
+    case QVNT_GATE_Z:  // z.rs: sign by parity
+        if (a) out.push_back(diag_gate(a, ctrl, {{1, 0}, {-1, 0}}, D_PAR));
+        return;
+    case QVNT_GATE_S: {  // s.rs: i^popcount (dagger: i^-popcount)
+        if (!a) return;
+        std::vector<C2> t;
+        const C2 p4[4] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
+        const int n = popc(a) == 1 ? 2 : 8;
+        for (int k = 0; k < n; ++k) t.push_back(p4[(g.dagger ? (8 - k) : k) & 3]);
+        out.push_back(diag_gate(a, ctrl, t, n == 2 ? D_PAR : D_POP));
+        return;
+    }
+    case QVNT_GATE_T: {  // t.rs: rotate(count >> 1), times e^{i pi/4} when count is odd
+        if (!a) return;
+        std::vector<C2> t;
+        const C2 p4[4] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
+        const int n = popc(a) == 1 ? 2 : 8;
+        for (int k = 0; k < n; ++k) {
+            const int kk = g.dagger ? ((8 - k) & 7) : k;
+            C2 z = p4[(kk >> 1) & 3];
+            if (kk & 1) z = C2{z.re * r - z.im * r, z.re * r + z.im * r};
+            t.push_back(z);
+        }
+        out.push_back(diag_gate(a, ctrl, t, n == 2 ? D_PAR : D_POP));
+        return;
+    }
+    case QVNT_GATE_RZ:   // rz.rs: (c, -s) where the bit is 0, (c, s) where it is 1
+    case QVNT_GATE_RZZ:  // rzz.rs: (c, -s) for even parity, (c, s) for odd
+        out.push_back(diag_gate(a, ctrl, {{c, -s}, {c, s}}, D_PAR));
+        return;
+    case QVNT_GATE_RX:  // rx.rs: c p0 - i s p1
+        out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_RX, c, -s, -s, c));
+        return;
+    case QVNT_GATE_RY:  // ry.rs: [[c, -s], [s, c]]
+        out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_REAL, c, -s, s, c));
+        return;
+    case QVNT_GATE_H1:  // h1.rs
+        out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_REAL, r, r, r, -r));
+        return;
+    case QVNT_GATE_H2:  // h2.rs = H on each of the two qubits
+        out.push_back(g1_gate(__builtin_ctzll(g.a_mask), ctrl, F_REAL, r, r, r, -r));
+        out.push_back(g1_gate(__builtin_ctzll(g.b_mask), ctrl, F_REAL, r, r, r, -r));
+        return;
+    case QVNT_GATE_U1: {  // u1.rs: dense 2x2
+        const double* m = g.matrix;
+        const bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
+        if (real) {
+            out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_REAL, m[0], m[2], m[4], m[6]));
+        } else {
+            EGate e;
+            e.op = OP_G1;
+            e.q0 = __builtin_ctzll(a);
+            e.ctrl = ctrl;
+            e.form0 = F_GEN;
+            for (int k = 0; k < 8; ++k) push_df(e.coef, m[k]);
+            e.cost = form_cost(F_GEN);
+            out.push_back(e);
+        }
+        return;
+    }
+    case QVNT_GATE_RXX: {  // rxx.rs: c p - i s p(partner) on both pairs
+        const C2 m[4] = {{c, 0}, {0, -s}, {0, -s}, {c, 0}};
+        out.push_back(g2p_gate(a, ctrl, F_RX, m, 0, F_RX, m, 0));
+        return;
+    }
+    case QVNT_GATE_RYY: {  // ryy.rs: c p - i pi p(partner), pi = -s on (00, 11), +s on (01, 10)
+        const C2 ma[4] = {{c, 0}, {0, s}, {0, s}, {c, 0}};
+        const C2 mb[4] = {{c, 0}, {0, -s}, {0, -s}, {c, 0}};
+        out.push_back(g2p_gate(a, ctrl, F_RX, ma, 0, F_RX, mb, 0));
+        return;
+    }
+    case QVNT_GATE_SWAP:  // swap.rs
+        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, F_PERM, nullptr, 0));
+        return;
+    case QVNT_GATE_ISWAP: {  // i_swap.rs: i p(partner) (dagger: -i)
+        const uint32_t code = g.dagger ? 3u : 1u;
+        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, F_PERM, nullptr, code | (code << 4)));
+        return;
+    }
+    case QVNT_GATE_SQRT_SWAP: {  // sqrt_swap.rs: 0.5(1+i) p + 0.5(1-i) p(partner) (dagger: conjugate)
+        const double sg = g.dagger ? -1.0 : 1.0;
+        const C2 m[4] = {{0.5, 0.5 * sg}, {0.5, -0.5 * sg}, {0.5, -0.5 * sg}, {0.5, 0.5 * sg}};
+        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, F_GEN, m, 0));
+        return;
+    }
+    case QVNT_GATE_SQRT_ISWAP: {  // sqrt_i_swap.rs: r p + i r p(partner) (dagger: -i r)
+        const double sg = g.dagger ? -1.0 : 1.0;
+        const C2 m[4] = {{r, 0}, {0, r * sg}, {0, r * sg}, {r, 0}};
+        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, F_RX, m, 0));
+        return;
+    }
+    case QVNT_GATE_U2: {  // u2.rs: dense 4x4, member index (b_bit << 1) | a_bit
+        EGate e;
+        const DevGate d = decode_gate(g);
+        if (plain_gate_needs_gather(d)) {
+            e.standalone = true;
+            e.src = src;
+            out.push_back(e);
+            return;
+        }
+        const int qa = __builtin_ctzll(g.a_mask), qb = __builtin_ctzll(g.b_mask);
+        e.op = OP_G4;
+        e.ctrl = ctrl;
+        e.q0 = std::min(qa, qb);
+        e.q1 = std::max(qa, qb);
+        // engine member order: (bit q0) | (bit q1) << 1; swap the roles of a and b when qa > qb
+        auto perm = [&](int r) { return qa < qb ? r : (((r & 1) << 1) | ((r >> 1) & 1)); };
+        for (int rr = 0; rr < 4; ++rr)
+            for (int cc = 0; cc < 4; ++cc) {
+                const int sr = perm(rr), sc = perm(cc);
+                push_df(e.coef, g.matrix[2 * (4 * sr + sc)]);
+                push_df(e.coef, g.matrix[2 * (4 * sr + sc) + 1]);
+            }
+        e.cost = 170;
+        out.push_back(e);
+        return;
+    }
+    default:
+        return;
+    }
+}
+
+uint64_t targets_of(const EGate& e) {
+    if (e.op == OP_DIAG || e.standalone) return 0;
+    uint64_t t = 1ull << e.q0;
+    if (e.q1 >= 0) t |= 1ull << e.q1;
+    return t;
+}
+
+uint64_t touched_of(const EGate& e) {
+    if (e.op == OP_DIAG) return e.dmask | e.ctrl;
+    return targets_of(e) | e.ctrl;
+}
+
+struct PlannedPass {
     bool standalone = false;
-    size_t gate = 0;  // standalone: index into the caller's list
+    size_t src = 0;
     uint64_t qmask = 0;
-    std::vector<size_t> members;
+    std::vector<size_t> members;  // indices into the engine gate list
 };
 
-uint32_t index_bits(uint64_t len) { return (uint32_t)__builtin_ctzll(len); }
+// Pass budget in estimated FP32 instructions per amplitude: about what one HBM round trip of the
+// tile hides at full bandwidth (32 B per amplitude at ~6.8 TB/s against ~114 FFMA/clk/SM).
+constexpr int kPassBudget = 220;
+constexpr size_t kLookahead = 2048;
 
 }  // namespace
 
@@ -230,159 +717,320 @@ void FusedState::release() {
     d_bytes = h_bytes = 0;
 }
 
-int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
-    const uint32_t L = index_bits(r->len);
-    uint32_t k = r->fusion_k ? r->fusion_k : kDefaultK;
-    if (k > L) k = L;
-    uint32_t c = k >= 10 ? 4 : (k >= 4 ? 2 : k);
-    if (c > k) c = k;
-    const uint64_t low = (1ull << c) - 1ull;
-    const uint64_t all = (L >= 64) ? ~0ull : ((1ull << L) - 1ull);
+int plan_fused(const qvnt_gate* gates, size_t count, uint32_t L, uint32_t fusion_k, std::vector<EGate>& eg,
+               std::vector<uint64_t>& tgt, std::vector<PlannedPass>& passes, uint32_t* kk_out) {
+    const uint32_t k = std::min<uint32_t>(fusion_k ? fusion_k : kTileQ, std::min<uint32_t>(L, kTileQ));
+    const uint32_t kk = std::max<uint32_t>(k, kRegQ);
+    // At least two free tile slots, so that every two-qubit gate fits an empty pass.
+    const uint32_t c0 = std::min<uint32_t>(kLowQ, kk - 2);
+    const uint64_t low = (1ull << c0) - 1ull;
+    const uint64_t all = (1ull << L) - 1ull;
+    *kk_out = kk;
 
-    // ---- plan ----
-    std::vector<GInfo> info(count);
-    for (size_t i = 0; i < count; ++i) info[i] = classify(gates[i], k, c);
-    std::vector<char> done(count, 0);
-    std::vector<Pass> passes;
+    // ---- lower ----
+    eg.clear();
+    eg.reserve(count * 2);
+    for (size_t i = 0; i < count; ++i) lower(gates[i], i, eg);
+    const size_t ne = eg.size();
+    std::vector<uint64_t> tch(ne);
+    tgt.assign(ne, 0);
+    for (size_t i = 0; i < ne; ++i) {
+        tgt[i] = targets_of(eg[i]);
+        // a standalone gate is an ordering barrier: nothing moves across it
+        tch[i] = eg[i].standalone ? ~0ull : touched_of(eg[i]);
+    }
+
+    // ---- plan passes ----
+    std::vector<char> done(ne, 0);
+    passes.clear();
     size_t first = 0;
     while (true) {
-        while (first < count && (done[first] || info[first].skip)) ++first;
-        if (first >= count) break;
-        if (info[first].standalone) {
-            Pass p;
+        while (first < ne && done[first]) ++first;
+        if (first >= ne) break;
+        if (eg[first].standalone) {
+            PlannedPass p;
             p.standalone = true;
-            p.gate = first;
+            p.src = eg[first].src;
             passes.push_back(p);
             done[first] = 1;
             continue;
         }
-        Pass p;
+        PlannedPass p;
         uint64_t Q = low;
-        uint32_t free_slots = k - c;
+        uint32_t free_slots = kk - c0;
         uint64_t block_nd = 0, block_d = 0;
-        size_t scanned = 0;
-        for (size_t j = first; j < count && scanned < kLookahead; ++j) {
-            if (done[j] || info[j].skip) continue;
+        int budget = 0;
+        size_t scanned = 0, ncoef = 0;
+        for (size_t j = first; j < ne && scanned < kLookahead; ++j) {
+            if (done[j]) continue;
             ++scanned;
-            const GInfo& g = info[j];
-            const bool conflict = g.diag ? (g.touched & block_nd) != 0 : (g.touched & (block_nd | block_d)) != 0;
-            if (!conflict && !g.standalone) {
-                const uint64_t need = g.targets & ~Q;
+            const EGate& g = eg[j];
+            const bool diag = g.op == OP_DIAG;
+            const bool conflict = diag ? (tch[j] & block_nd) != 0 : (tch[j] & (block_nd | block_d)) != 0;
+            bool take = false;
+            if (!conflict && !g.standalone && budget + g.cost <= kPassBudget && p.members.size() < (size_t)kMaxGates &&
+                ncoef + g.coef.size() <= (size_t)kMaxCoef) {
+                const uint64_t need = tgt[j] & ~Q;
                 if (popc(need) <= free_slots) {
                     Q |= need;
                     free_slots -= popc(need);
-                    p.members.push_back(j);
-                    done[j] = 1;
-                    continue;
+                    take = true;
                 }
             }
-            if (g.diag) block_d |= g.touched;
-            else block_nd |= g.touched;
+            if (take) {
+                p.members.push_back(j);
+                done[j] = 1;
+                budget += g.cost;
+                ncoef += g.coef.size();
+                continue;
+            }
+            if (diag) block_d |= tch[j];
+            else block_nd |= tch[j];
             if ((block_nd & all) == all) break;
+            if (budget >= kPassBudget) break;
         }
-        // Fill unused tile slots with the lowest free qubits: longer contiguous runs per tile.
         for (uint32_t b = 0; b < L && free_slots > 0; ++b)
             if (!((Q >> b) & 1ull)) {
                 Q |= 1ull << b;
                 --free_slots;
             }
+        if (p.members.empty())
+            return set_error(QVNT_ERR_UNSUPPORTED, "fused planner could not place engine gate %zu", first);
         p.qmask = Q;
         passes.push_back(p);
     }
-    if (passes.empty()) return QVNT_OK;
+    return QVNT_OK;
+}
 
-    // ---- lower and upload ----
-    size_t nl = 0;
-    for (const Pass& p : passes) nl += p.members.size();
-    const size_t bytes = std::max<size_t>(nl, 1) * sizeof(LGate);
-    if (r->fused.h_buf && r->fused.h_bytes < bytes) {
-        cudaStreamSynchronize(r->stream);
-        cudaFreeHost(r->fused.h_buf);
-        r->fused.h_buf = nullptr;
-    }
-    if (!r->fused.h_buf) {
-        QVNT_CUDA_TRY(cudaMallocHost(&r->fused.h_buf, bytes));
-        r->fused.h_bytes = bytes;
-    } else {
-        // The previous upload from this pinned buffer must have completed before it is rewritten.
-        QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));
-    }
-    if (r->fused.d_bytes < bytes) {
-        QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));
-        if (r->fused.d_buf) cudaFree(r->fused.d_buf);
-        r->fused.d_buf = nullptr;
-        cudaError_t e = cudaMalloc(&r->fused.d_buf, bytes);
-        if (e != cudaSuccess) return set_cuda_error(e, "cudaMalloc(pass descriptors)");
-        r->fused.d_bytes = bytes;
-    }
-    LGate* hl = reinterpret_cast<LGate*>(r->fused.h_buf);
-    std::vector<TileGeom> geoms(passes.size());
-    std::vector<size_t> offs(passes.size());
-    size_t at = 0;
-    for (size_t pi = 0; pi < passes.size(); ++pi) {
-        const Pass& p = passes[pi];
-        if (p.standalone) continue;
-        TileGeom tg;
-        memset(&tg, 0, sizeof tg);
-        uint32_t n = 0;
-        for (uint32_t b = 0; b < L; ++b)
-            if ((p.qmask >> b) & 1ull) tg.qpos[n++] = b;
-        tg.k = n;
-        uint32_t run = 0;
-        while (run < n && tg.qpos[run] == run) ++run;
-        tg.c = run;
-        tg.nhigh = n - run;
-        for (uint32_t j = 0; j < tg.nhigh; ++j) tg.high[j] = tg.qpos[run + j];
-        Enum te{};
-        te.nins = n;
-        for (uint32_t j = 0; j < n; ++j) te.ins[j] = tg.qpos[j];
-        te.ones = 0;
-        te.count = r->len >> n;
-        tg.tiles = te;
-        geoms[pi] = tg;
-        offs[pi] = at;
-        for (size_t m : p.members) hl[at++] = lower_gate(gates[m], tg.qpos, n, p.qmask);
-    }
-    if (at) QVNT_CUDA_TRY(cudaMemcpyAsync(r->fused.d_buf, hl, at * sizeof(LGate), cudaMemcpyHostToDevice, r->stream));
-
-    // ---- launch ----
-    const LGate* dl = reinterpret_cast<const LGate*>(r->fused.d_buf);
-    for (size_t pi = 0; pi < passes.size(); ++pi) {
-        const Pass& p = passes[pi];
-        cudaEvent_t stop = nullptr;  // timing covers the fused-pass kernel only
-        int st = QVNT_OK;
+template <class F>
+int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>& eg, const std::vector<uint64_t>& tgt,
+                  const std::vector<PlannedPass>& passes, uint32_t kk, F&& standalone_gate) {
+    const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
+    PassParams* P = new PassParams;
+    int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
+    const size_t smem = ((size_t)1 << kk) * 16;
+    if (smem > 48 * 1024)
+        QVNT_CUDA_TRY(cudaFuncSetAttribute(fused_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int status = QVNT_OK;
+    for (const PlannedPass& p : passes) {
         if (p.standalone) {
-            DevGate d = decode_gate(gates[p.gate]);
-            if (plain_gate_needs_gather(d)) {
-                st = reg_ensure_alt(r);
-                if (st) return st;
-                st = launch_gather_gate(r->psi, r->alt, r->len, d, r->stream, r->ctx->geo);
-                std::swap(r->psi, r->alt);
-            } else {
-                st = launch_plain_gate(r->psi, r->len, d, r->stream, r->ctx->geo);
-            }
-            if (st) return st;
-        } else {
-            const TileGeom& tg = geoms[pi];
-            const size_t smem = ((size_t)1 << tg.k) * sizeof(amp_t) + ((size_t)1 << tg.nhigh) * sizeof(uint64_t);
-            if (smem > 48 * 1024)
-                QVNT_CUDA_TRY(cudaFuncSetAttribute(fused_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)smem));
-            const int per_sm = std::max(1, (int)((size_t)(r->ctx->smem_optin ? r->ctx->smem_optin : 48 * 1024) / smem));
-            uint64_t grid = (uint64_t)r->ctx->geo.sms * std::min(per_sm, 4);
-            if (grid > tg.tiles.count) grid = tg.tiles.count;
-            st = timing_begin(r, &stop);
-            if (st) return st;
-            fused_pass_kernel<<<(unsigned)grid, kFusedThreads, smem, r->stream>>>(r->psi, dl + offs[pi],
-                                                                                 (uint32_t)p.members.size(), tg);
-            QVNT_CUDA_TRY(cudaGetLastError());
+            status = standalone_gate(gates[p.src]);
+            if (status) break;
+            continue;
         }
-        st = timing_end(r, stop);
-        if (st) return st;
+        memset(P, 0, sizeof(PassParams));
+        uint32_t n = 0;
+        uint32_t pos_of[64];
+        for (uint32_t b = 0; b < L; ++b)
+            if ((p.qmask >> b) & 1ull) {
+                pos_of[b] = n;
+                P->tq[n++] = b;
+            }
+        uint32_t run = 0;
+        while (run < n && P->tq[run] == run) ++run;
+        P->k = n;
+        P->c = std::min<uint32_t>(run, n);
+        P->nthreads = 1u << (n - kRegQ);
+        P->ntiles = r->len >> n;
+        auto local = [&](uint64_t m) {  // global mask (within Q) -> tile-local mask
+            uint32_t lm = 0;
+            for (uint32_t b = 0; b < L; ++b)
+                if (((m & p.qmask) >> b) & 1ull) lm |= 1u << pos_of[b];
+            return lm;
+        };
+        // stages: contiguous runs of members whose targets fit 4 register bits
+        std::vector<std::pair<uint32_t, std::vector<size_t>>> stages;  // (register local mask, gates)
+        for (size_t m : p.members) {
+            const uint32_t lt = local(tgt[m]);
+            if (stages.empty() || (eg[m].op != OP_DIAG && popc(stages.back().first | lt) > (unsigned)kRegQ))
+                stages.push_back({lt, {}});
+            else
+                stages.back().first |= lt;
+            stages.back().second.push_back(m);
+        }
+        if (stages.size() > (size_t)kMaxStages) {
+            status = set_error(QVNT_ERR_UNSUPPORTED, "pass needs %zu stages", stages.size());
+            break;
+        }
+        P->nstages = (uint32_t)stages.size();
+        uint32_t ng = 0, nc = 0;
+        for (size_t si = 0; si < stages.size(); ++si) {
+            uint32_t R = stages[si].first;
+            // fill the register bits with the highest free tile bits (keeps lanes on low tile bits)
+            for (int b = (int)n - 1; b >= 0 && popc(R) < (unsigned)kRegQ; --b)
+                if (!((R >> b) & 1u)) R |= 1u << b;
+            DStage& S = P->stages[si];
+            uint32_t nb = 0, nt = 0;
+            uint32_t rix[kTileQ], tix[kTileQ];
+            for (uint32_t b = 0; b < n; ++b) {
+                if ((R >> b) & 1u) {
+                    rix[b] = nb;
+                    S.rbit[nb++] = (uint8_t)b;
+                } else {
+                    tix[b] = nt;
+                    S.tbit[nt++] = (uint8_t)b;
+                }
+            }
+            S.gbegin = (uint16_t)ng;
+            for (size_t m : stages[si].second) {
+                const EGate& e = eg[m];
+                DGate& G = P->gates[ng++];
+                G.op = e.op;
+                G.form0 = e.form0;
+                G.form1 = e.form1;
+                G.dkind = e.dkind;
+                G.exact = e.exact ? 1 : 0;
+                G.codes = e.codes;
+                G.coef = nc;
+                for (float f : e.coef) P->coef[nc++] = f;
+                const uint32_t lc = local(e.ctrl);
+                G.ctrl_out = e.ctrl & ~p.qmask;
+                uint32_t creg = 0, cthr = 0;
+                for (uint32_t b = 0; b < n; ++b)
+                    if ((lc >> b) & 1u) {
+                        if ((R >> b) & 1u) creg |= 1u << rix[b];
+                        else cthr |= 1u << tix[b];
+                    }
+                G.ctrl_reg = (uint8_t)creg;
+                G.ctrl_thr = (uint16_t)cthr;
+                if (e.op == OP_DIAG) {
+                    const uint32_t ld = local(e.dmask);
+                    G.dm_out = e.dmask & ~p.qmask;
+                    uint32_t dreg = 0, dthr = 0;
+                    for (uint32_t b = 0; b < n; ++b)
+                        if ((ld >> b) & 1u) {
+                            if ((R >> b) & 1u) dreg |= 1u << rix[b];
+                            else dthr |= 1u << tix[b];
+                        }
+                    G.dm_reg = (uint8_t)dreg;
+                    G.dm_thr = (uint16_t)dthr;
+                } else {
+                    G.b0 = (uint8_t)rix[pos_of[e.q0]];
+                    if (e.q1 >= 0) G.b1 = (uint8_t)rix[pos_of[e.q1]];
+                    if (e.q1 >= 0 && G.b0 > G.b1) {
+                        // register order differs from qubit order: only symmetric blocks reach here for
+                        // G2P; G4 matrices are permuted to register order
+                        std::swap(G.b0, G.b1);
+                        if (e.op == OP_G4) {
+                            float tmp[64];
+                            memcpy(tmp, &P->coef[G.coef], sizeof tmp);
+                            auto perm = [](int x) { return ((x & 1) << 1) | ((x >> 1) & 1); };
+                            for (int rr = 0; rr < 4; ++rr)
+                                for (int cc = 0; cc < 4; ++cc)
+                                    for (int w = 0; w < 4; ++w)
+                                        P->coef[G.coef + 16 * rr + 4 * cc + w] = tmp[16 * perm(rr) + 4 * perm(cc) + w];
+                        }
+                    }
+                }
+            }
+            S.gend = (uint16_t)ng;
+        }
+        const int per_sm = 2;
+        uint64_t grid = (uint64_t)r->ctx->geo.sms * per_sm;
+        if (grid > P->ntiles) grid = P->ntiles;
+        cudaEvent_t stop = nullptr;
+        status = timing_begin(r, &stop);
+        if (status) break;
+        fused_df_kernel<<<(unsigned)grid, P->nthreads, smem, r->stream>>>(reinterpret_cast<float4*>(r->psi), *P,
+                                                                          d_err);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            status = set_cuda_error(e, "fused_df_kernel launch");
+            break;
+        }
+        status = timing_end(r, stop);
+        if (status) break;
         r->launches += 1;
         r->passes += 1;
     }
+    delete P;
+    return status;
+}
+int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
+    const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
+    const int fmt = FMT_DF64;
+    // Registers below 4 qubits of index space run per-gate passes.
+    auto standalone_gate = [&](const qvnt_gate& g) -> int {
+        DevGate d = decode_gate(g);
+        if (plain_gate_is_identity(d)) return QVNT_OK;
+        int st;
+        if (plain_gate_needs_gather(d)) {
+            st = reg_ensure_alt(r);
+            if (st) return st;
+            st = launch_gather_gate(r->psi, r->alt, fmt, r->len, d, r->stream, r->ctx->geo);
+            std::swap(r->psi, r->alt);
+        } else {
+            st = launch_plain_gate(r->psi, fmt, r->len, d, r->stream, r->ctx->geo);
+        }
+        r->launches += 1;
+        r->passes += 1;
+        return st;
+    };
+    if (L < (uint32_t)kRegQ) {
+        for (size_t i = 0; i < count; ++i) {
+            int st = standalone_gate(gates[i]);
+            if (st) return st;
+        }
+        return QVNT_OK;
+    }
+    std::vector<EGate> eg;
+    std::vector<uint64_t> tgt, tch;
+    std::vector<PlannedPass> passes;
+    uint32_t kk = 0;
+    int status = plan_fused(gates, count, L, r->fusion_k, eg, tgt, passes, &kk);
+    if (status) return status;
+    return launch_passes(r, gates, eg, tgt, passes, kk, standalone_gate);
+}
+
+
+}  // namespace qvnt
+
+using namespace qvnt;
+
+extern "C" int qvnt_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint32_t fusion_k,
+                              uint64_t* passes, uint64_t* stages, uint64_t* engine_gates) {
+    if (!gates && count) return set_error(QVNT_ERR_BAD_ARG, "null gate list");
+    if (q_num > 40) return set_error(QVNT_ERR_BAD_ARG, "q_num %u > 40", q_num);
+    const uint64_t len = q_num < 3 ? 8 : (1ull << q_num);
+    for (size_t k = 0; k < count; ++k) {
+        int st = validate_gate(gates[k], len);
+        if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
+    }
+    const uint32_t L = (uint32_t)__builtin_ctzll(len);
+    uint64_t np = 0, ns = 0, nq = 0;
+    if (L < (uint32_t)kRegQ) {
+        np = count;
+    } else {
+        std::vector<EGate> eg;
+        std::vector<uint64_t> tgt;
+        std::vector<PlannedPass> pl;
+        uint32_t kk = 0;
+        int st = plan_fused(gates, count, L, fusion_k, eg, tgt, pl, &kk);
+        if (st) return st;
+        np = pl.size();
+        nq = eg.size();
+        for (const PlannedPass& p : pl) {
+            if (p.standalone) continue;
+            // same grouping as launch_passes: a stage holds gates whose targets fit 4 register bits
+            uint64_t cur = 0;
+            bool open = false;
+            for (size_t m : p.members) {
+                if (!open || (eg[m].op != OP_DIAG && __builtin_popcountll(cur | tgt[m]) > kRegQ)) {
+                    ++ns;
+                    open = true;
+                    cur = tgt[m];
+                } else {
+                    cur |= tgt[m];
+                }
+            }
+        }
+    }
+    if (passes) *passes = np;
+    if (stages) *stages = ns;
+    if (engine_gates) *engine_gates = nq;
     return QVNT_OK;
 }
+
+namespace qvnt {
 
 }  // namespace qvnt

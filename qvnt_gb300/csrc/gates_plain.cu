@@ -6,11 +6,14 @@
 // same `atomic_op` expression for every member and stores the results in place.  Orbits are
 // enumerated by bit insertion: the target bits are inserted as 0 and the control bits as 1 into a
 // dense counter, so a gate with c controls touches only 2^(n-c) amplitudes.  Built with
-// --fmad=false: results are bit-identical to qvnt's non-fast-math arithmetic.
+// --fmad=false: on IEEE f64 storage the results are bit-identical to qvnt's non-fast-math
+// arithmetic.  The same kernels serve double-float registers for gates the fused engine does not
+// tile (AccDF64 converts on load and store).
 #include <algorithm>
 #include <vector>
 
 #include "atomic.cuh"
+#include "df64.cuh"
 #include "kernels.h"
 
 namespace qvnt {
@@ -19,9 +22,9 @@ namespace {
 
 constexpr int kUnroll = 2;
 
-template <int SHAPE>
-__global__ void __launch_bounds__(256) plain_gate_kernel(amp_t* __restrict__ psi, const DevGate g,
-                                                         const Enum e, const uint64_t pmask) {
+template <int SHAPE, class Acc>
+__global__ void __launch_bounds__(256) plain_gate_kernel(double2* __restrict__ psi, const DevGate g, const Enum e,
+                                                         const uint64_t pmask) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t j0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j0 < e.count; j0 += stride * kUnroll) {
         amp_t v[kUnroll][SHAPE];
@@ -32,15 +35,15 @@ __global__ void __launch_bounds__(256) plain_gate_kernel(amp_t* __restrict__ psi
             if (j < e.count) {
                 base[u] = enum_index(e, j);
                 if (SHAPE == 1) {
-                    v[u][0] = psi[base[u]];
+                    v[u][0] = Acc::load(psi, base[u]);
                 } else if (SHAPE == 2) {
-                    v[u][0] = psi[base[u]];
-                    v[u][1] = psi[base[u] ^ pmask];
+                    v[u][0] = Acc::load(psi, base[u]);
+                    v[u][1] = Acc::load(psi, base[u] ^ pmask);
                 } else {
-                    v[u][0] = psi[base[u]];
-                    v[u][1] = psi[base[u] | g.a];
-                    v[u][2] = psi[base[u] | g.b];
-                    v[u][3] = psi[base[u] | g.a | g.b];
+                    v[u][0] = Acc::load(psi, base[u]);
+                    v[u][1] = Acc::load(psi, base[u] | g.a);
+                    v[u][2] = Acc::load(psi, base[u] | g.b);
+                    v[u][3] = Acc::load(psi, base[u] | g.a | g.b);
                 }
             }
         }
@@ -51,15 +54,15 @@ __global__ void __launch_bounds__(256) plain_gate_kernel(amp_t* __restrict__ psi
             const uint64_t i0 = base[u];
             if (SHAPE == 1) {
                 const amp_t x = v[u][0];
-                psi[i0] = atomic_op(g, i0, [&](uint64_t) { return x; });
+                Acc::store(psi, i0, atomic_op(g, i0, [&](uint64_t) { return x; }));
             } else if (SHAPE == 2) {
                 const amp_t x0 = v[u][0], x1 = v[u][1];
                 const uint64_t i1 = i0 ^ pmask;
                 auto f = [&](uint64_t k) { return k == i0 ? x0 : x1; };
                 const amp_t o0 = atomic_op(g, i0, f);
                 const amp_t o1 = atomic_op(g, i1, f);
-                psi[i0] = o0;
-                psi[i1] = o1;
+                Acc::store(psi, i0, o0);
+                Acc::store(psi, i1, o1);
             } else {
                 const amp_t x0 = v[u][0], x1 = v[u][1], x2 = v[u][2], x3 = v[u][3];
                 const uint64_t a = g.a, b = g.b;
@@ -71,10 +74,10 @@ __global__ void __launch_bounds__(256) plain_gate_kernel(amp_t* __restrict__ psi
                 const amp_t o1 = atomic_op(g, i0 | a, f);
                 const amp_t o2 = atomic_op(g, i0 | b, f);
                 const amp_t o3 = atomic_op(g, i0 | a | b, f);
-                psi[i0] = o0;
-                psi[i0 | a] = o1;
-                psi[i0 | b] = o2;
-                psi[i0 | a | b] = o3;
+                Acc::store(psi, i0, o0);
+                Acc::store(psi, i0 | a, o1);
+                Acc::store(psi, i0 | b, o2);
+                Acc::store(psi, i0 | a | b, o3);
             }
         }
     }
@@ -82,14 +85,15 @@ __global__ void __launch_bounds__(256) plain_gate_kernel(amp_t* __restrict__ psi
 
 // qvnt's own out-of-place gather, for gates whose orbits are not closed (a U2 controlled on its
 // own b qubit, which qvnt allows because u2 `acts_on` omits b_mask, u2.rs:70-72).
-__global__ void __launch_bounds__(256) gather_gate_kernel(const amp_t* __restrict__ in, amp_t* __restrict__ out,
+template <class Acc>
+__global__ void __launch_bounds__(256) gather_gate_kernel(const double2* __restrict__ in, double2* __restrict__ out,
                                                           const DevGate g, const uint64_t len) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < len; idx += stride) {
         if ((~idx & g.ctrl) == 0)
-            out[idx] = atomic_op(g, idx, [&](uint64_t k) { return in[k]; });
+            Acc::store(out, idx, atomic_op(g, idx, [&](uint64_t k) { return Acc::load(in, k); }));
         else
-            out[idx] = in[idx];
+            Acc::store(out, idx, Acc::load(in, idx));
     }
 }
 
@@ -116,6 +120,15 @@ unsigned grid_for(uint64_t work, const Geometry& geo, int threads) {
     return (unsigned)want;
 }
 
+template <int SHAPE>
+void launch_shape(int fmt, unsigned grid, cudaStream_t stream, double2* psi, const DevGate& g, const Enum& e,
+                  uint64_t pmask) {
+    if (fmt == FMT_DF64)
+        plain_gate_kernel<SHAPE, AccDF64><<<grid, 256, 0, stream>>>(psi, g, e, pmask);
+    else
+        plain_gate_kernel<SHAPE, AccF64><<<grid, 256, 0, stream>>>(psi, g, e, pmask);
+}
+
 }  // namespace
 
 bool plain_gate_is_identity(const DevGate& g) {
@@ -131,32 +144,33 @@ bool plain_gate_is_identity(const DevGate& g) {
 
 bool plain_gate_needs_gather(const DevGate& g) { return g.kind == QVNT_GATE_U2 && (g.ctrl & g.b) != 0; }
 
-int launch_plain_gate(amp_t* psi, uint64_t len, const DevGate& g, cudaStream_t stream, const Geometry& geo) {
+int launch_plain_gate(double2* psi, int fmt, uint64_t len, const DevGate& g, cudaStream_t stream,
+                      const Geometry& geo) {
     const int threads = 256;
     const uint64_t ctrl = g.ctrl;
     switch (g.kind) {
     case QVNT_GATE_Z: case QVNT_GATE_S: case QVNT_GATE_T: case QVNT_GATE_RZ: case QVNT_GATE_RZZ: {
         Enum e = make_enum(len, ctrl, ctrl);
-        plain_gate_kernel<1><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, 0);
+        launch_shape<1>(fmt, grid_for(e.count, geo, threads), stream, psi, g, e, 0);
         break;
     }
     case QVNT_GATE_X: case QVNT_GATE_Y: case QVNT_GATE_RX: case QVNT_GATE_RY: case QVNT_GATE_H1:
     case QVNT_GATE_U1: case QVNT_GATE_RXX: case QVNT_GATE_RYY: {
         const uint64_t pivot = 1ull << high_bit(g.a);
         Enum e = make_enum(len, ctrl | pivot, ctrl);
-        plain_gate_kernel<2><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, g.a);
+        launch_shape<2>(fmt, grid_for(e.count, geo, threads), stream, psi, g, e, g.a);
         break;
     }
     case QVNT_GATE_SWAP: case QVNT_GATE_ISWAP: case QVNT_GATE_SQRT_SWAP: case QVNT_GATE_SQRT_ISWAP: {
         // Only members with odd parity of idx & ab change (swap.rs:17): pair (01) <-> (10).
         const uint64_t lo = 1ull << low_bit(g.a);
         Enum e = make_enum(len, ctrl | g.a, ctrl | lo);
-        plain_gate_kernel<2><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, g.a);
+        launch_shape<2>(fmt, grid_for(e.count, geo, threads), stream, psi, g, e, g.a);
         break;
     }
     case QVNT_GATE_H2: case QVNT_GATE_U2: {
         Enum e = make_enum(len, ctrl | g.a | g.b, ctrl);
-        plain_gate_kernel<4><<<grid_for(e.count, geo, threads), threads, 0, stream>>>(psi, g, e, 0);
+        launch_shape<4>(fmt, grid_for(e.count, geo, threads), stream, psi, g, e, 0);
         break;
     }
     default:
@@ -166,10 +180,13 @@ int launch_plain_gate(amp_t* psi, uint64_t len, const DevGate& g, cudaStream_t s
     return QVNT_OK;
 }
 
-int launch_gather_gate(const amp_t* in, amp_t* out, uint64_t len, const DevGate& g, cudaStream_t stream,
+int launch_gather_gate(const double2* in, double2* out, int fmt, uint64_t len, const DevGate& g, cudaStream_t stream,
                        const Geometry& geo) {
     const int threads = 256;
-    gather_gate_kernel<<<grid_for(len, geo, threads), threads, 0, stream>>>(in, out, g, len);
+    if (fmt == FMT_DF64)
+        gather_gate_kernel<AccDF64><<<grid_for(len, geo, threads), threads, 0, stream>>>(in, out, g, len);
+    else
+        gather_gate_kernel<AccF64><<<grid_for(len, geo, threads), threads, 0, stream>>>(in, out, g, len);
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }

@@ -1,21 +1,25 @@
-// Register-wide passes: norm, probabilities, measure_mask, collapse, normalize, reset, tensor.
+// Register-wide passes: norm, probabilities, measure_mask, collapse, normalize, reset, tensor and
+// storage-format conversion.
 //
-// Built with --fmad=false so that |psi|^2 = re*re + im*im and p_i = |psi_i|^2 * (1/sum) round as
-// qvnt's `norm_sqr` and `get_probabilities` do (src/register/quant.rs:434-454).  Sums are taken in
-// a fixed tree order (chunk partials, then one block), so every result is reproducible run to run.
+// Every kernel reads amplitudes through an accessor (AccF64: IEEE f64 storage of the plain engine;
+// AccDF64: double-float storage of the fused engine) and computes in FP64.  Built with --fmad=false
+// so that |psi|^2 = re*re + im*im and p_i = |psi_i|^2 * (1/sum) round as qvnt's `norm_sqr` and
+// `get_probabilities` do (src/register/quant.rs:434-454).  Sums are taken in a fixed tree order
+// (chunk partials, then one block): results are reproducible run to run.
 #include <math.h>
 
 #include "atomic.cuh"
+#include "df64.cuh"
 #include "kernels.h"
 
 namespace qvnt {
 
 namespace {
 
-constexpr int kRedThreads = 256;   // chunk reduction block
-constexpr int kScanThreads = 1024; // single-block search
+constexpr int kRedThreads = 256;    // chunk reduction block
+constexpr int kScanThreads = 1024;  // single-block search
 
-__device__ __forceinline__ double nsq(amp_t z) { return z.x * z.x + z.y * z.y; }
+__device__ __forceinline__ double nsq(double2 z) { return z.x * z.x + z.y * z.y; }
 
 template <int THREADS>
 __device__ __forceinline__ double block_sum(double v, double* sm) {
@@ -34,8 +38,7 @@ __device__ __forceinline__ double block_sum(double v, double* sm) {
     return t;  // valid in thread 0
 }
 
-// Inclusive scan over the block in thread order; returns this thread's inclusive prefix and the
-// block total in *total.
+// Inclusive scan over the block in thread order; *total gets the block total.
 template <int THREADS>
 __device__ __forceinline__ double block_inclusive_scan(double v, double* sm, double* total) {
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -62,8 +65,9 @@ __device__ __forceinline__ double block_inclusive_scan(double v, double* sm, dou
     return v;
 }
 
-// Partial sums per chunk of kChunk amplitudes: sum_i |psi_i|^2 * scale over i < limit.
-__global__ void __launch_bounds__(kRedThreads) chunk_sum_kernel(const amp_t* __restrict__ psi, uint64_t limit,
+// Partial sums per chunk of kChunk amplitudes: sum_i |psi_i|^2 (* scale) over i < limit.
+template <class Acc>
+__global__ void __launch_bounds__(kRedThreads) chunk_sum_kernel(const double2* __restrict__ psi, uint64_t limit,
                                                                  const double* __restrict__ d_scale,
                                                                  double* __restrict__ partial) {
     __shared__ double sm[32];
@@ -72,7 +76,7 @@ __global__ void __launch_bounds__(kRedThreads) chunk_sum_kernel(const amp_t* __r
     double s = 0.0;
     for (uint32_t k = threadIdx.x; k < kChunk; k += kRedThreads) {
         const uint64_t i = base + k;
-        if (i < limit) s += d_scale ? nsq(psi[i]) * scale : nsq(psi[i]);
+        if (i < limit) s += d_scale ? nsq(Acc::load(psi, i)) * scale : nsq(Acc::load(psi, i));
     }
     double t = block_sum<kRedThreads>(s, sm);
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
@@ -97,7 +101,8 @@ __global__ void inv_kernel(const double* d_abs, double* d_inv, int* d_status) {
 // WeightedIndex selection (rand 0.8.5): first i with inclusive cumulative p > u01 * total,
 // i <= q_size - 2, else q_size - 1.  One block: chunk-level prefix, then element-level prefix
 // inside the crossing chunk.
-__global__ void __launch_bounds__(kScanThreads) search_kernel(const amp_t* __restrict__ psi, uint64_t q_size,
+template <class Acc>
+__global__ void __launch_bounds__(kScanThreads) search_kernel(const double2* __restrict__ psi, uint64_t q_size,
                                                                const double* __restrict__ pchunk,
                                                                const double* __restrict__ d_inv, double u01,
                                                                uint64_t* __restrict__ d_idx) {
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(kScanThreads) search_kernel(const amp_t* __res
 #pragma unroll
     for (int k = 0; k < per_t; ++k) {
         const uint64_t i = e0 + k;
-        p[k] = (i < q_size) ? nsq(psi[i]) * inv : 0.0;
+        p[k] = (i < q_size) ? nsq(Acc::load(psi, i)) * inv : 0.0;
         ls += p[k];
     }
     __syncthreads();
@@ -185,68 +190,105 @@ __global__ void __launch_bounds__(kScanThreads) search_kernel(const amp_t* __res
     }
 }
 
-__global__ void collapse_kernel(amp_t* __restrict__ psi, uint64_t len, const uint64_t* __restrict__ d_idx,
+template <class Acc>
+__global__ void collapse_kernel(double2* __restrict__ psi, uint64_t len, const uint64_t* __restrict__ d_idx,
                                 uint64_t mask) {
     const uint64_t idy = *d_idx;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
-        if (((i ^ idy) & mask) != 0) psi[i] = make_double2(0.0, 0.0);
+        if (((i ^ idy) & mask) != 0) Acc::store(psi, i, make_double2(0.0, 0.0));
 }
 
-__global__ void scale_kernel(amp_t* __restrict__ psi, uint64_t len, const double* __restrict__ d_abs, int mode) {
-    // mode 0: qvnt `normalize` thresholds; mode 1: always rescale to unit norm (renormalise).
+template <class Acc>
+__global__ void scale_kernel(double2* __restrict__ psi, uint64_t len, const double* __restrict__ d_abs, int mode) {
+    // mode 0: qvnt `normalize` thresholds (quant.rs:397-414); mode 1: always rescale to unit norm.
     const double norm = sqrt(*d_abs);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     if (norm <= 1e-15) {
         if (mode == 1) return;
         for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
-            psi[i] = make_double2(i == 0 ? 1.0 : 0.0, 0.0);
+            Acc::store(psi, i, make_double2(i == 0 ? 1.0 : 0.0, 0.0));
         return;
     }
     if (mode == 0 && 1. - norm <= 1e-9) return;
     const double inv = 1. / norm;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride) {
-        amp_t v = psi[i];
-        psi[i] = make_double2(v.x * inv, v.y * inv);
+        double2 v = Acc::load(psi, i);
+        Acc::store(psi, i, make_double2(v.x * inv, v.y * inv));
     }
 }
 
-__global__ void prob_kernel(const amp_t* __restrict__ psi, uint64_t first, uint64_t count,
+template <class Acc>
+__global__ void prob_kernel(const double2* __restrict__ psi, uint64_t first, uint64_t count,
                             const double* __restrict__ d_inv, double* __restrict__ out) {
     const double inv = *d_inv;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride)
-        out[k] = nsq(psi[first + k]) * inv;
+        out[k] = nsq(Acc::load(psi, first + k)) * inv;
 }
 
-__global__ void polar_kernel(const amp_t* __restrict__ psi, uint64_t first, uint64_t count, double* __restrict__ out) {
+template <class Acc>
+__global__ void polar_kernel(const double2* __restrict__ psi, uint64_t first, uint64_t count, double* __restrict__ out) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
-        amp_t v = psi[first + k];
+        double2 v = Acc::load(psi, first + k);
         out[2 * k] = hypot(v.x, v.y);
         out[2 * k + 1] = atan2(v.y, v.x);
     }
 }
 
-__global__ void reset_kernel(amp_t* __restrict__ psi, uint64_t len, uint64_t state) {
+template <class Acc>
+__global__ void copy_out_kernel(const double2* __restrict__ psi, uint64_t first, uint64_t count,
+                                double2* __restrict__ out) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
-        psi[i] = make_double2(i == state ? 1.0 : 0.0, 0.0);
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride)
+        out[k] = Acc::load(psi, first + k);
 }
 
-__global__ void zero_mask_kernel(amp_t* __restrict__ psi, uint64_t len, uint64_t mask) {
+template <class Acc>
+__global__ void copy_in_kernel(double2* __restrict__ psi, uint64_t first, uint64_t count,
+                               const double2* __restrict__ in) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
-        if (i & mask) psi[i] = make_double2(0.0, 0.0);
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride)
+        Acc::store(psi, first + k, in[k]);
 }
 
-__global__ void tensor_kernel(const amp_t* __restrict__ a, uint32_t na, const amp_t* __restrict__ b, uint32_t nb,
-                              amp_t* __restrict__ out, uint64_t out_len) {
+template <class Acc>
+__global__ void reset_kernel(double2* __restrict__ psi, uint64_t len, uint64_t state) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        Acc::store(psi, i, make_double2(i == state ? 1.0 : 0.0, 0.0));
+}
+
+template <class Acc>
+__global__ void zero_mask_kernel(double2* __restrict__ psi, uint64_t len, uint64_t mask) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        if (i & mask) Acc::store(psi, i, make_double2(0.0, 0.0));
+}
+
+template <class AccA, class AccB, class AccO>
+__global__ void tensor_kernel(const double2* __restrict__ a, uint32_t na, const double2* __restrict__ b, uint32_t nb,
+                              double2* __restrict__ out, uint64_t out_len) {
     const uint64_t q_size = 1ull << (na + nb);
     const uint64_t ma = (1ull << na) - 1, mb = (1ull << nb) - 1;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < out_len; i += stride)
-        out[i] = i < q_size ? c_mul(a[i & ma], b[(i >> na) & mb]) : make_double2(0.0, 0.0);
+        AccO::store(out, i, i < q_size ? c_mul(AccA::load(a, i & ma), AccB::load(b, (i >> na) & mb))
+                                       : make_double2(0.0, 0.0));
+}
+
+// Storage conversion in place: f64 -> df64 (to_df = 1) or df64 -> f64 (to_df = 0).
+__global__ void convert_kernel(double2* __restrict__ psi, uint64_t len, int to_df) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride) {
+        if (to_df) {
+            const double2 v = psi[i];
+            AccDF64::store(psi, i, v);
+        } else {
+            psi[i] = AccDF64::load(psi, i);
+        }
+    }
 }
 
 unsigned flat_grid(uint64_t n) {
@@ -256,41 +298,41 @@ unsigned flat_grid(uint64_t n) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
+#define QVNT_BY_FMT(fmt, KERNEL, ...)                 \
+    do {                                              \
+        if ((fmt) == FMT_DF64) KERNEL<AccDF64> __VA_ARGS__; \
+        else KERNEL<AccF64> __VA_ARGS__;              \
+    } while (0)
+
 }  // namespace
 
-int launch_norm_sqr_sum(const amp_t* psi, uint64_t len, double* scratch, double* d_out, cudaStream_t stream) {
+int launch_norm_sqr_sum(const double2* psi, int fmt, uint64_t len, double* scratch, double* d_out, cudaStream_t stream) {
     const uint64_t nc = chunk_count(len);
-    chunk_sum_kernel<<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, scratch);
+    QVNT_BY_FMT(fmt, chunk_sum_kernel, <<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, scratch));
     final_sum_kernel<<<1, kScanThreads, 0, stream>>>(scratch, nc, d_out);
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }
 
-int launch_measure(amp_t* psi, uint64_t len, uint64_t q_size, uint64_t mask, double u01, double* scratch,
+int launch_measure(double2* psi, int fmt, uint64_t len, uint64_t q_size, uint64_t mask, double u01, double* scratch,
                    uint64_t* d_idx, int* d_status, int renormalise, cudaStream_t stream) {
     const uint64_t nc = chunk_count(len);
     double* partial = scratch;
     double* pchunk = scratch + nc;
     double* d_abs = scratch + 2 * nc;
     double* d_inv = d_abs + 1;
-    chunk_sum_kernel<<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, partial);
+    QVNT_BY_FMT(fmt, chunk_sum_kernel, <<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, partial));
     final_sum_kernel<<<1, kScanThreads, 0, stream>>>(partial, nc, d_abs);
     inv_kernel<<<1, 1, 0, stream>>>(d_abs, d_inv, d_status);
-    chunk_sum_kernel<<<(unsigned)chunk_count(q_size), kRedThreads, 0, stream>>>(psi, q_size, d_inv, pchunk);
-    search_kernel<<<1, kScanThreads, 0, stream>>>(psi, q_size, pchunk, d_inv, u01, d_idx);
-    collapse_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, d_idx, mask);
+    QVNT_BY_FMT(fmt, chunk_sum_kernel,
+                <<<(unsigned)chunk_count(q_size), kRedThreads, 0, stream>>>(psi, q_size, d_inv, pchunk));
+    QVNT_BY_FMT(fmt, search_kernel, <<<1, kScanThreads, 0, stream>>>(psi, q_size, pchunk, d_inv, u01, d_idx));
+    QVNT_BY_FMT(fmt, collapse_kernel, <<<flat_grid(len), 256, 0, stream>>>(psi, len, d_idx, mask));
     if (renormalise) {
-        chunk_sum_kernel<<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, partial);
+        QVNT_BY_FMT(fmt, chunk_sum_kernel, <<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, len, nullptr, partial));
         final_sum_kernel<<<1, kScanThreads, 0, stream>>>(partial, nc, d_abs);
-        scale_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, d_abs, 1);
+        QVNT_BY_FMT(fmt, scale_kernel, <<<flat_grid(len), 256, 0, stream>>>(psi, len, d_abs, 1));
     }
-    QVNT_CUDA_TRY(cudaGetLastError());
-    return QVNT_OK;
-}
-
-int launch_probabilities(const amp_t* psi, uint64_t first, uint64_t count, const double* d_inv_abs,
-                         double* d_out, cudaStream_t stream) {
-    prob_kernel<<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_inv_abs, d_out);
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }
@@ -301,33 +343,69 @@ int launch_inv(const double* d_abs, double* d_inv, int* d_status, cudaStream_t s
     return QVNT_OK;
 }
 
-int launch_polar(const amp_t* psi, uint64_t first, uint64_t count, double* d_out, cudaStream_t stream) {
-    polar_kernel<<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_out);
+int launch_probabilities(const double2* psi, int fmt, uint64_t first, uint64_t count, const double* d_inv_abs,
+                         double* d_out, cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, prob_kernel, <<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_inv_abs, d_out));
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }
 
-int launch_reset(amp_t* psi, uint64_t len, uint64_t state, cudaStream_t stream) {
-    reset_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, state);
+int launch_polar(const double2* psi, int fmt, uint64_t first, uint64_t count, double* d_out, cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, polar_kernel, <<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_out));
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }
 
-int launch_zero_mask(amp_t* psi, uint64_t len, uint64_t mask, cudaStream_t stream) {
-    zero_mask_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, mask);
+int launch_copy_out(const double2* psi, int fmt, uint64_t first, uint64_t count, double2* d_out, cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, copy_out_kernel, <<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_out));
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }
 
-int launch_normalize(amp_t* psi, uint64_t len, const double* d_abs, cudaStream_t stream) {
-    scale_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, d_abs, 0);
+int launch_copy_in(double2* psi, int fmt, uint64_t first, uint64_t count, const double2* d_in, cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, copy_in_kernel, <<<flat_grid(count), 256, 0, stream>>>(psi, first, count, d_in));
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }
 
-int launch_tensor(const amp_t* a, uint32_t na, const amp_t* b, uint32_t nb, amp_t* out, uint64_t out_len,
-                  cudaStream_t stream) {
-    tensor_kernel<<<flat_grid(out_len), 256, 0, stream>>>(a, na, b, nb, out, out_len);
+int launch_reset(double2* psi, int fmt, uint64_t len, uint64_t state, cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, reset_kernel, <<<flat_grid(len), 256, 0, stream>>>(psi, len, state));
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_zero_mask(double2* psi, int fmt, uint64_t len, uint64_t mask, cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, zero_mask_kernel, <<<flat_grid(len), 256, 0, stream>>>(psi, len, mask));
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_normalize(double2* psi, int fmt, uint64_t len, const double* d_abs, cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, scale_kernel, <<<flat_grid(len), 256, 0, stream>>>(psi, len, d_abs, 0));
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_tensor(const double2* a, int fa, uint32_t na, const double2* b, int fb, uint32_t nb, double2* out, int fo,
+                  uint64_t out_len, cudaStream_t stream) {
+    const unsigned g = flat_grid(out_len);
+    const int code = (fa << 2) | (fb << 1) | fo;
+    switch (code) {
+    case 0: tensor_kernel<AccF64, AccF64, AccF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    case 1: tensor_kernel<AccF64, AccF64, AccDF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    case 2: tensor_kernel<AccF64, AccDF64, AccF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    case 3: tensor_kernel<AccF64, AccDF64, AccDF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    case 4: tensor_kernel<AccDF64, AccF64, AccF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    case 5: tensor_kernel<AccDF64, AccF64, AccDF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    case 6: tensor_kernel<AccDF64, AccDF64, AccF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    default: tensor_kernel<AccDF64, AccDF64, AccDF64><<<g, 256, 0, stream>>>(a, na, b, nb, out, out_len); break;
+    }
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_convert(double2* psi, uint64_t len, int to_df, cudaStream_t stream) {
+    convert_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, to_df);
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }

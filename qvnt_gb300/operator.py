@@ -155,6 +155,16 @@ class MultiOp:
         return [[complex(cols[c][r]) for c in range(dim)] for r in range(dim)]
 
 
+def plan_info(ops, q_num, fusion_k=0):
+    """How the fused engine would run `ops` on a q_num-qubit register (host-side planning only):
+    (passes, register stages, engine gates)."""
+    gates = ops.gates()
+    arr = _abi.gate_array(gates)
+    p, s, e = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().qvnt_plan_info(arr, len(gates), q_num, fusion_k, ctypes.byref(p), ctypes.byref(s), ctypes.byref(e)))
+    return p.value, s.value, e.value
+
+
 def _list(builder, *args):
     count = ctypes.c_size_t()
     check(builder(*args, None, 0, ctypes.byref(count)))

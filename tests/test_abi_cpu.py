@@ -146,3 +146,20 @@ def test_circuit_sizes(lib_built):
     assert 1600 <= len(c1) <= 1620
     c2 = random_circuit(30, 40, seed=2)
     assert 2800 <= len(c2) <= 3200
+
+
+def test_fused_planner_terminates_and_covers(lib_built):
+    """The fused planner runs on the host: every gate list gets a finite plan at every tile width."""
+    from qvnt_gb300.circuits import plain_circuit, random_circuit
+    from test_gpu_parity import all_kinds_circuit
+    for n in (3, 4, 5, 7, 12, 14, 20):
+        circ = all_kinds_circuit(max(n, 3), 300, seed=n)
+        for k in (0, 6, 8, 10, 12, 13):
+            passes, stages, eg = op.plan_info(circ, n, k)
+            assert 0 < passes <= max(eg, 1) + len(circ)
+            if n >= 4:
+                assert stages >= passes - len(circ)
+    p30, s30, e30 = op.plan_info(random_circuit(30, 40, seed=2), 30)
+    assert p30 < e30
+    p20, _, _ = op.plan_info(plain_circuit(20, 20, seed=1), 20)
+    assert p20 < 1610
