@@ -63,8 +63,12 @@ __device__ __forceinline__ df df_mul(df c, df x) {
 }
 
 // Sum of N unnormalised terms: hi parts through a two_sum chain, all error parts summed in float.
+// The result is left UNNORMALISED (hi = the rounded sum of the hi parts, lo = everything else): the
+// gate kernels renormalise once per register stage (df_renorm) instead of after every gate.  Until
+// then |lo| stays within a few ulp(hi) of the inputs' magnitude, so the absolute error of every
+// later error-free product stays at ~2^-48 of the amplitudes involved.
 template <int N>
-__device__ __forceinline__ df df_sum(const df (&t)[N]) {
+__device__ __forceinline__ df df_sum_raw(const df (&t)[N]) {
     float s = t[0].h;
     float e = t[0].l;
 #pragma unroll
@@ -73,19 +77,38 @@ __device__ __forceinline__ df df_sum(const df (&t)[N]) {
         s = q.h;
         e = __fadd_rn(e, __fadd_rn(q.l, t[k].l));
     }
-    return fast_two_sum(s, e);
+    return df{s, e};
 }
 
-// c0*x0 + c1*x1 (real df constants, df values).
+template <int N>
+__device__ __forceinline__ df df_sum(const df (&t)[N]) {
+    const df r = df_sum_raw<N>(t);
+    return fast_two_sum(r.h, r.l);
+}
+
+// Renormalisation of an unnormalised pair (no magnitude assumption).
+__device__ __forceinline__ df df_renorm(df a) { return two_sum(a.h, a.l); }
+
+// c0*x0 + c1*x1 (real df constants, df values), unnormalised.
 __device__ __forceinline__ df df_lin2(df c0, df x0, df c1, df x1) {
     const df t[2] = {df_mul_raw(c0, x0), df_mul_raw(c1, x1)};
-    return df_sum<2>(t);
+    return df_sum_raw<2>(t);
 }
 
-// c0*x0 + c1*x1 + c2*x2 + c3*x3.
+// c0*x0 + c1*x1 + c2*x2 + c3*x3, unnormalised.
 __device__ __forceinline__ df df_lin4(df c0, df x0, df c1, df x1, df c2, df x2, df c3, df x3) {
     const df t[4] = {df_mul_raw(c0, x0), df_mul_raw(c1, x1), df_mul_raw(c2, x2), df_mul_raw(c3, x3)};
-    return df_sum<4>(t);
+    return df_sum_raw<4>(t);
+}
+
+// x0 + x1 and x0 - x1 (the unscaled Hadamard butterfly), unnormalised.
+__device__ __forceinline__ df df_add_raw(df a, df b) {
+    const df s = two_sum(a.h, b.h);
+    return df{s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l))};
+}
+__device__ __forceinline__ df df_sub_raw(df a, df b) {
+    const df s = two_sum(a.h, -b.h);
+    return df{s.h, __fadd_rn(s.l, __fsub_rn(a.l, b.l))};
 }
 
 // Complex multiply by a df complex constant: (cr + i ci) * (xr + i xi).

@@ -2,21 +2,25 @@
 // double-float arithmetic (df64.cuh) on the FP32 pipes.
 //
 // qvnt applies every SingleOp as a full sweep over the state (src/operator/multi/mod.rs:97-114).
-// Here the host plans PASSES.  A pass picks k = 12 tile qubits Q, always containing the five lowest
-// qubits, so a tile -- the 2^12 amplitudes that share all non-Q index bits -- is 2^(12-5) contiguous
-// 512-byte runs.  Each CTA (256 threads, persistent over tiles):
+// Here the host plans PASSES.  A pass picks KT tile qubits Q (12 by default), always containing the
+// lowest qubits, so a tile -- the 2^KT amplitudes that share all non-Q index bits -- is a set of
+// contiguous runs of at least 512 bytes.  Each CTA (persistent over tiles):
 //   1. stages the tile into shared memory with TMA bulk copies (cp.async.bulk, one per run) that
-//      complete on an mbarrier;
-//   2. runs the pass's STAGES: a stage gives every thread 16 amplitudes in registers, spanning 4
+//      complete on an mbarrier (bounded wait, error flag on timeout);
+//   2. runs the pass's STAGES: a stage gives every thread 2^KR amplitudes in registers, spanning KR
 //      "register qubits" of the tile, applies every gate of the stage there, and writes back;
 //   3. writes the tile back with TMA bulk stores.
 // A gate joins a pass when its target qubits lie in Q; controls may lie anywhere (outside Q they
 // are a per-tile predicate, on thread bits a per-thread predicate) and diagonal gates (Z, S, T, RZ,
 // RZZ) join any pass and any stage.  A gate may overtake a deferred gate only when both are diagonal
 // or their qubit supports are disjoint, so the result is the in-order product up to rounding.
+// Uncontrolled Hadamards run as unscaled butterflies; their 2^(-m/2) is applied once per pass.
+// Runs of one-qubit gates on the same qubit (u3 = rz ry rz, rx ry rz, ...) are merged on the host
+// into one 2x2 matrix when that costs fewer instructions.
 // The pass descriptor (stages, gates, coefficients) is a __grid_constant__ kernel parameter.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -28,18 +32,22 @@ namespace qvnt {
 
 namespace {
 
-constexpr int kTileQ = 12;                         // qubits per tile
-constexpr int kRegQ = 4;                           // register qubits per thread
-constexpr int kSlots = 1 << kRegQ;                 // amplitudes per thread
-constexpr int kMaxThreads = 1 << (kTileQ - kRegQ);  // 256
-constexpr int kLowQ = 5;                           // lowest qubits always in a tile (512-byte runs)
+constexpr int kMaxKT = 12;   // largest tile (qubits)
+constexpr int kMaxKR = 4;    // largest register-qubit count
+constexpr int kLowQ = 5;     // lowest qubits always in a tile (512-byte runs)
 constexpr int kMaxGates = 192;
 constexpr int kMaxStages = 96;
 constexpr int kMaxCoef = 4096;
 constexpr uint32_t kWaitLimit = 1u << 22;  // bounded mbarrier waits (iterations of try_wait)
 
-enum : uint8_t { OP_G1 = 1, OP_G2P = 2, OP_G4 = 3, OP_DIAG = 4 };
-enum : uint8_t { F_ID = 0, F_PERM = 1, F_RX = 2, F_REAL = 3, F_GEN = 4 };
+// OP_DIAG1: a diagonal gate on ONE qubit (two table entries by that bit); its register bit, or the
+// thread / out-of-tile bit it reads, is resolved per stage so that no per-amplitude select is left.
+enum : uint8_t { OP_G1 = 1, OP_G2P = 2, OP_G4 = 3, OP_DIAG = 4, OP_DIAG1 = 5 };
+// Exact permutation forms are compile-time specialisations: F_SWAPX [[0,1],[1,0]] (X, SWAP),
+// F_PY [[0,-i],[i,0]] (Y), F_PI [[0,i],[i,0]] (iSWAP), F_PMI [[0,-i],[-i,0]] (iSWAP dagger);
+// F_PERM is any other pair of powers of i.
+enum : uint8_t { F_ID = 0, F_PERM = 1, F_RX = 2, F_REAL = 3, F_GEN = 4, F_HADD = 5, F_SWAPX = 6, F_PY = 7,
+                 F_PI = 8, F_PMI = 9 };
 enum : uint8_t { D_PAR = 0, D_POP = 1 };
 
 struct DGate {
@@ -53,24 +61,28 @@ struct DGate {
     uint8_t dm_reg;     // diagonal mask on register bits
     uint8_t op, form0, form1, b0, b1, dkind;
     uint8_t exact;      // diagonal: every table entry is a power of i
-    uint8_t pad[7];
+    uint8_t one0;       // OP_DIAG1: table entry 0 is exactly 1 (nothing to do where the bit is 0)
+    uint8_t pad[6];
 };
 static_assert(sizeof(DGate) == 48, "DGate layout");
 
 struct DStage {
-    uint8_t rbit[kRegQ];   // tile-local bit of register bit b
-    uint8_t tbit[kTileQ - kRegQ];  // tile-local bit of thread bit i
+    uint8_t rbit[kMaxKR];   // tile-local bit of register bit b
+    uint8_t tbit[kMaxKT];   // tile-local bit of thread bit i
     uint16_t gbegin, gend;
 };
-static_assert(sizeof(DStage) == 16, "DStage layout");
+static_assert(sizeof(DStage) == 20, "DStage layout");
 
 struct PassParams {
     uint64_t ntiles;
-    uint32_t k;        // tile qubits of this pass (<= 12)
-    uint32_t c;        // contiguous low run: tile-local bits 0..c-1 are qubits 0..c-1
-    uint32_t nthreads;  // 2^(k - 4)
+    uint32_t k;         // tile qubits of this pass
+    uint32_t c;         // contiguous low run: tile-local bits 0..c-1 are qubits 0..c-1
+    uint32_t nthreads;  // 2^(k - KR)
     uint32_t nstages;
-    uint32_t tq[kTileQ];   // global qubit of tile-local bit p (ascending)
+    uint32_t tq[kMaxKT];  // global qubit of tile-local bit p (ascending)
+    float scale_h, scale_l;  // deferred Hadamard factor 2^(-m/2) as a df pair
+    uint32_t has_scale;
+    uint32_t pad;
     DStage stages[kMaxStages];
     DGate gates[kMaxGates];
     float coef[kMaxCoef];
@@ -117,12 +129,38 @@ __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_
 // ---- register-level gate application ------------------------------------------------------------
 __device__ __forceinline__ df cdf(const PassParams& P, uint32_t o) { return df{P.coef[o], P.coef[o + 1]}; }
 
-// One 2x2 block on the pair (x0, x1): [y0; y1] = M [x0; x1].
+// z * i^Q for a compile-time Q: register renames and sign flips only.
+template <int Q>
+__device__ __forceinline__ dfc rotc(dfc z) {
+    if (Q == 1) return dfc{df_neg(z.im), z.re};
+    if (Q == 2) return dfc{df_neg(z.re), df_neg(z.im)};
+    if (Q == 3) return dfc{z.im, df_neg(z.re)};
+    return z;
+}
+
+// One 2x2 block on the pair (x0, x1): [y0; y1] = M [x0; x1]; results are left unnormalised.
 template <int FORM>
 __device__ __forceinline__ void pair_op(dfc& x0, dfc& x1, const PassParams& P, uint32_t o, uint32_t codes) {
-    if (FORM == F_PERM) {
+    if (FORM == F_SWAPX) {
+        const dfc t = x0;
+        x0 = x1;
+        x1 = t;
+    } else if (FORM == F_PY || FORM == F_PI || FORM == F_PMI) {
+        const dfc n0 = rotc<FORM == F_PI ? 1 : 3>(x1);
+        const dfc n1 = rotc<FORM == F_PMI ? 3 : 1>(x0);
+        x0 = n0;
+        x1 = n1;
+    } else if (FORM == F_PERM) {
         const dfc n0 = dfc_rotate(x1, codes & 3u);
         const dfc n1 = dfc_rotate(x0, (codes >> 4) & 3u);
+        x0 = n0;
+        x1 = n1;
+    } else if (FORM == F_HADD) {
+        dfc n0, n1;
+        n0.re = df_add_raw(x0.re, x1.re);
+        n0.im = df_add_raw(x0.im, x1.im);
+        n1.re = df_sub_raw(x0.re, x1.re);
+        n1.im = df_sub_raw(x0.im, x1.im);
         x0 = n0;
         x1 = n1;
     } else if (FORM == F_RX) {
@@ -157,35 +195,43 @@ __device__ __forceinline__ void pair_op(dfc& x0, dfc& x1, const PassParams& P, u
     }
 }
 
-template <int B, int FORM>
-__device__ __forceinline__ void g1_form(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
+template <int SLOTS, int B, int FORM>
+__device__ __forceinline__ void g1_form(dfc (&v)[SLOTS], const PassParams& P, const DGate& G) {
     const uint32_t creg = G.ctrl_reg;
+    if (creg == 0) {
 #pragma unroll
-    for (int j = 0; j < kSlots; ++j) {
-        if (j & (1 << B)) continue;
-        if (tok && (j & creg) == creg) pair_op<FORM>(v[j], v[j | (1 << B)], P, G.coef, G.codes);
+        for (int j = 0; j < SLOTS; ++j)
+            if (!(j & (1 << B))) pair_op<FORM>(v[j], v[j | (1 << B)], P, G.coef, G.codes);
+    } else {
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j)
+            if (!(j & (1 << B)) && (j & creg) == creg) pair_op<FORM>(v[j], v[j | (1 << B)], P, G.coef, G.codes);
     }
 }
 
-template <int B>
-__device__ __forceinline__ void g1(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
+template <int SLOTS, int B>
+__device__ __forceinline__ void g1(dfc (&v)[SLOTS], const PassParams& P, const DGate& G) {
     switch (G.form0) {
-    case F_PERM: g1_form<B, F_PERM>(v, P, G, tok); break;
-    case F_RX: g1_form<B, F_RX>(v, P, G, tok); break;
-    case F_REAL: g1_form<B, F_REAL>(v, P, G, tok); break;
-    default: g1_form<B, F_GEN>(v, P, G, tok); break;
+    case F_SWAPX: g1_form<SLOTS, B, F_SWAPX>(v, P, G); break;
+    case F_PY: g1_form<SLOTS, B, F_PY>(v, P, G); break;
+    case F_PI: g1_form<SLOTS, B, F_PI>(v, P, G); break;
+    case F_PMI: g1_form<SLOTS, B, F_PMI>(v, P, G); break;
+    case F_HADD: g1_form<SLOTS, B, F_HADD>(v, P, G); break;
+    case F_RX: g1_form<SLOTS, B, F_RX>(v, P, G); break;
+    case F_REAL: g1_form<SLOTS, B, F_REAL>(v, P, G); break;
+    default: g1_form<SLOTS, B, F_GEN>(v, P, G); break;
     }
 }
 
 // Two-qubit gate as 2x2 blocks on the pairs (00, 11) [block A] and (01, 10) [block B] of register
 // bits B0 < B1; member order inside a pair: the one with bit B0 clear in A, set in B, first.
-template <int B0, int B1, int FORM>
-__device__ __forceinline__ void g2p_block(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok,
+template <int SLOTS, int B0, int B1, int FORM>
+__device__ __forceinline__ void g2p_block(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, bool tok,
                                           bool blockA, uint32_t o, uint32_t codes) {
     constexpr int M0 = 1 << B0, M1 = 1 << B1;
     const uint32_t creg = G.ctrl_reg;
 #pragma unroll
-    for (int j = 0; j < kSlots; ++j) {
+    for (int j = 0; j < SLOTS; ++j) {
         if (j & (M0 | M1)) continue;
         if (!(tok && (j & creg) == creg)) continue;
         if (blockA)
@@ -195,34 +241,36 @@ __device__ __forceinline__ void g2p_block(dfc (&v)[kSlots], const PassParams& P,
     }
 }
 
-template <int B0, int B1>
-__device__ __forceinline__ void g2p_any(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok, bool blockA) {
+template <int SLOTS, int B0, int B1>
+__device__ __forceinline__ void g2p_any(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, bool tok, bool blockA) {
     const uint8_t form = blockA ? G.form0 : G.form1;
     const uint32_t o = G.coef + (blockA ? 0u : 16u);
     const uint32_t codes = blockA ? (G.codes & 0xffu) : ((G.codes >> 8) & 0xffu);
     switch (form) {
     case F_ID: break;
-    case F_PERM: g2p_block<B0, B1, F_PERM>(v, P, G, tok, blockA, o, codes); break;
-    case F_RX: g2p_block<B0, B1, F_RX>(v, P, G, tok, blockA, o, codes); break;
-    case F_REAL: g2p_block<B0, B1, F_REAL>(v, P, G, tok, blockA, o, codes); break;
-    default: g2p_block<B0, B1, F_GEN>(v, P, G, tok, blockA, o, codes); break;
+    case F_SWAPX: g2p_block<SLOTS, B0, B1, F_SWAPX>(v, P, G, tok, blockA, o, codes); break;
+    case F_PI: g2p_block<SLOTS, B0, B1, F_PI>(v, P, G, tok, blockA, o, codes); break;
+    case F_PMI: g2p_block<SLOTS, B0, B1, F_PMI>(v, P, G, tok, blockA, o, codes); break;
+    case F_RX: g2p_block<SLOTS, B0, B1, F_RX>(v, P, G, tok, blockA, o, codes); break;
+    case F_REAL: g2p_block<SLOTS, B0, B1, F_REAL>(v, P, G, tok, blockA, o, codes); break;
+    default: g2p_block<SLOTS, B0, B1, F_GEN>(v, P, G, tok, blockA, o, codes); break;
     }
 }
 
-template <int B0, int B1>
-__device__ __forceinline__ void g2p(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
-    g2p_any<B0, B1>(v, P, G, tok, true);
-    g2p_any<B0, B1>(v, P, G, tok, false);
+template <int SLOTS, int B0, int B1>
+__device__ __forceinline__ void g2p(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, bool tok) {
+    g2p_any<SLOTS, B0, B1>(v, P, G, tok, true);
+    g2p_any<SLOTS, B0, B1>(v, P, G, tok, false);
 }
 
 // Dense 4x4 on register bits B0 < B1; member r = (bit B0) | (bit B1) << 1, row-major complex matrix.
-template <int B0, int B1>
-__device__ __forceinline__ void g4(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok) {
+template <int SLOTS, int B0, int B1>
+__device__ __forceinline__ void g4(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, bool tok) {
     constexpr int M0 = 1 << B0, M1 = 1 << B1;
     const uint32_t creg = G.ctrl_reg;
     const uint32_t o = G.coef;
 #pragma unroll
-    for (int j = 0; j < kSlots; ++j) {
+    for (int j = 0; j < SLOTS; ++j) {
         if (j & (M0 | M1)) continue;
         if (!(tok && (j & creg) == creg)) continue;
         const int s[4] = {j, j | M0, j | M1, j | M0 | M1};
@@ -240,13 +288,14 @@ __device__ __forceinline__ void g4(dfc (&v)[kSlots], const PassParams& P, const 
                 ti[2 * c] = df_mul_raw(mr, x[c].im);
                 ti[2 * c + 1] = df_mul_raw(mi, x[c].re);
             }
-            v[s[r]].re = df_sum<8>(tr);
-            v[s[r]].im = df_sum<8>(ti);
+            v[s[r]].re = df_sum_raw<8>(tr);
+            v[s[r]].im = df_sum_raw<8>(ti);
         }
     }
 }
 
-__device__ __forceinline__ void gdiag(dfc (&v)[kSlots], const PassParams& P, const DGate& G, bool tok, uint32_t tid,
+template <int SLOTS>
+__device__ __forceinline__ void gdiag(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, bool tok, uint32_t tid,
                                       uint64_t base) {
     if (!tok) return;
     const uint32_t cnt0 = __popc(tid & G.dm_thr) + __popcll(base & G.dm_out);
@@ -255,7 +304,7 @@ __device__ __forceinline__ void gdiag(dfc (&v)[kSlots], const PassParams& P, con
         const uint32_t codes = G.codes;
         const uint32_t idxmask = G.dkind == D_PAR ? 1u : 7u;
 #pragma unroll
-        for (int j = 0; j < kSlots; ++j) {
+        for (int j = 0; j < SLOTS; ++j) {
             if ((j & creg) != creg) continue;
             const uint32_t k = (cnt0 + __popc(j & dreg)) & idxmask;
             v[j] = dfc_rotate(v[j], (codes >> (4 * k)) & 3u);
@@ -264,14 +313,14 @@ __device__ __forceinline__ void gdiag(dfc (&v)[kSlots], const PassParams& P, con
         const uint32_t o = G.coef;
         const df r0 = cdf(P, o), i0 = cdf(P, o + 2), r1 = cdf(P, o + 4), i1 = cdf(P, o + 6);
 #pragma unroll
-        for (int j = 0; j < kSlots; ++j) {
+        for (int j = 0; j < SLOTS; ++j) {
             if ((j & creg) != creg) continue;
             const bool odd = (cnt0 + __popc(j & dreg)) & 1u;
             v[j] = dfc_mul(odd ? r1 : r0, odd ? i1 : i0, v[j]);
         }
     } else {
 #pragma unroll
-        for (int j = 0; j < kSlots; ++j) {
+        for (int j = 0; j < SLOTS; ++j) {
             if ((j & creg) != creg) continue;
             const uint32_t o = G.coef + 4u * ((cnt0 + __popc(j & dreg)) & 7u);
             v[j] = dfc_mul(cdf(P, o), cdf(P, o + 2), v[j]);
@@ -279,17 +328,113 @@ __device__ __forceinline__ void gdiag(dfc (&v)[kSlots], const PassParams& P, con
     }
 }
 
-__device__ __forceinline__ void apply_gate(dfc (&v)[kSlots], const PassParams& P, const DGate& G, uint32_t tid,
+// Applies a compile-time power of i to the slots whose register bit B equals VAL (and controls hold).
+template <int SLOTS, int B, int VAL, int Q>
+__device__ __forceinline__ void rot_slots(dfc (&v)[SLOTS], uint32_t creg) {
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j)
+        if (((j >> B) & 1) == VAL && (j & creg) == creg) v[j] = rotc<Q>(v[j]);
+}
+
+template <int SLOTS, int B, int VAL>
+__device__ __forceinline__ void rot_slots_code(dfc (&v)[SLOTS], uint32_t creg, uint32_t code) {
+    switch (code & 3u) {
+    case 1: rot_slots<SLOTS, B, VAL, 1>(v, creg); break;
+    case 2: rot_slots<SLOTS, B, VAL, 2>(v, creg); break;
+    case 3: rot_slots<SLOTS, B, VAL, 3>(v, creg); break;
+    default: break;
+    }
+}
+
+// One-qubit diagonal on register bit B: entry 1 where the bit is set, entry 0 elsewhere.
+template <int SLOTS, int B>
+__device__ __forceinline__ void diag1_reg(dfc (&v)[SLOTS], const PassParams& P, const DGate& G) {
+    const uint32_t creg = G.ctrl_reg;
+    if (G.exact) {
+        rot_slots_code<SLOTS, B, 1>(v, creg, G.codes >> 4);
+        rot_slots_code<SLOTS, B, 0>(v, creg, G.codes);
+        return;
+    }
+    const uint32_t o = G.coef;
+    const df r1 = cdf(P, o + 4), i1 = cdf(P, o + 6);
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j)
+        if (((j >> B) & 1) && (j & creg) == creg) v[j] = dfc_mul(r1, i1, v[j]);
+    if (!G.one0) {
+        const df r0 = cdf(P, o), i0 = cdf(P, o + 2);
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j)
+            if (!((j >> B) & 1) && (j & creg) == creg) v[j] = dfc_mul(r0, i0, v[j]);
+    }
+}
+
+// One-qubit diagonal on a thread bit or a bit outside the tile: one phase for all slots of a thread.
+template <int SLOTS>
+__device__ __forceinline__ void diag1_uniform(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, uint32_t tid,
+                                              uint64_t base) {
+    const uint32_t creg = G.ctrl_reg;
+    const bool bit = (tid & G.dm_thr) != 0 || (base & G.dm_out) != 0;
+    if (G.exact) {
+        // a per-thread switch over compile-time rotations: no per-slot selects
+        switch ((bit ? (G.codes >> 4) : G.codes) & 3u) {
+        case 1:
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j)
+                if ((j & creg) == creg) v[j] = rotc<1>(v[j]);
+            break;
+        case 2:
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j)
+                if ((j & creg) == creg) v[j] = rotc<2>(v[j]);
+            break;
+        case 3:
+#pragma unroll
+            for (int j = 0; j < SLOTS; ++j)
+                if ((j & creg) == creg) v[j] = rotc<3>(v[j]);
+            break;
+        default:
+            break;
+        }
+        return;
+    }
+    if (!bit && G.one0) return;
+    const uint32_t o = G.coef + (bit ? 4u : 0u);
+    const df cr = cdf(P, o), ci = cdf(P, o + 2);
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j)
+        if ((j & creg) == creg) v[j] = dfc_mul(cr, ci, v[j]);
+}
+
+template <int KR>
+__device__ __forceinline__ void apply_gate(dfc (&v)[1 << KR], const PassParams& P, const DGate& G, uint32_t tid,
                                            uint64_t base) {
+    constexpr int S = 1 << KR;
     if ((base & G.ctrl_out) != G.ctrl_out) return;
-    const bool tok = (tid & G.ctrl_thr) == G.ctrl_thr;
+    if ((tid & G.ctrl_thr) != G.ctrl_thr) return;
+    const bool tok = true;
     switch (G.op) {
     case OP_G1:
         switch (G.b0) {
-        case 0: g1<0>(v, P, G, tok); break;
-        case 1: g1<1>(v, P, G, tok); break;
-        case 2: g1<2>(v, P, G, tok); break;
-        default: g1<3>(v, P, G, tok); break;
+        case 0: g1<S, 0>(v, P, G); break;
+        case 1: g1<S, 1>(v, P, G); break;
+        case 2: g1<S, 2>(v, P, G); break;
+        default:
+            if constexpr (KR > 3) g1<S, 3>(v, P, G);
+            break;
+        }
+        break;
+    case OP_DIAG1:
+        if (G.dm_reg) {
+            switch (G.b0) {
+            case 0: diag1_reg<S, 0>(v, P, G); break;
+            case 1: diag1_reg<S, 1>(v, P, G); break;
+            case 2: diag1_reg<S, 2>(v, P, G); break;
+            default:
+                if constexpr (KR > 3) diag1_reg<S, 3>(v, P, G);
+                break;
+            }
+        } else {
+            diag1_uniform<S>(v, P, G, tid, base);
         }
         break;
     case OP_G2P:
@@ -297,31 +442,41 @@ __device__ __forceinline__ void apply_gate(dfc (&v)[kSlots], const PassParams& P
         const int pr = G.b0 * 4 + G.b1;
         const bool d = G.op == OP_G4;
         switch (pr) {
-        case 1: d ? g4<0, 1>(v, P, G, tok) : g2p<0, 1>(v, P, G, tok); break;
-        case 2: d ? g4<0, 2>(v, P, G, tok) : g2p<0, 2>(v, P, G, tok); break;
-        case 3: d ? g4<0, 3>(v, P, G, tok) : g2p<0, 3>(v, P, G, tok); break;
-        case 6: d ? g4<1, 2>(v, P, G, tok) : g2p<1, 2>(v, P, G, tok); break;
-        case 7: d ? g4<1, 3>(v, P, G, tok) : g2p<1, 3>(v, P, G, tok); break;
-        default: d ? g4<2, 3>(v, P, G, tok) : g2p<2, 3>(v, P, G, tok); break;
+        case 1: d ? g4<S, 0, 1>(v, P, G, tok) : g2p<S, 0, 1>(v, P, G, tok); break;
+        case 2: d ? g4<S, 0, 2>(v, P, G, tok) : g2p<S, 0, 2>(v, P, G, tok); break;
+        case 6: d ? g4<S, 1, 2>(v, P, G, tok) : g2p<S, 1, 2>(v, P, G, tok); break;
+        default:
+            if constexpr (KR > 3) {
+                switch (pr) {
+                case 3: d ? g4<S, 0, 3>(v, P, G, tok) : g2p<S, 0, 3>(v, P, G, tok); break;
+                case 7: d ? g4<S, 1, 3>(v, P, G, tok) : g2p<S, 1, 3>(v, P, G, tok); break;
+                default: d ? g4<S, 2, 3>(v, P, G, tok) : g2p<S, 2, 3>(v, P, G, tok); break;
+                }
+            }
+            break;
         }
         break;
     }
     default:
-        gdiag(v, P, G, tok, tid, base);
+        gdiag<S>(v, P, G, tok, tid, base);
         break;
     }
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 2)
+template <int KT, int KR, int MINB>
+__global__ void __launch_bounds__(1 << (KT - KR), MINB)
     fused_df_kernel(float4* __restrict__ psi, const __grid_constant__ PassParams P, int* __restrict__ err) {
+    constexpr int SLOTS = 1 << KR;
+    constexpr int NTB = KT - KR;  // thread bits
     extern __shared__ __align__(128) float4 tile[];
-    __shared__ uint64_t seg_off[1 << (kTileQ - kLowQ)];
+    __shared__ uint64_t seg_off[1 << (kMaxKT - kLowQ)];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ int s_abort;
     const uint32_t tid = threadIdx.x;
     const uint32_t nthr = P.nthreads;
     const uint32_t nseg = 1u << (P.k - P.c);
     const uint32_t seg_amps = 1u << P.c;
+    const uint32_t lanes = nthr < 32 ? nthr : 32;
     for (uint32_t s = tid; s < nseg; s += nthr) {
         uint64_t off = 0;
         for (uint32_t j = 0; j < P.k - P.c; ++j)
@@ -334,6 +489,7 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         s_abort = 0;
     }
     __syncthreads();
+    const df scale{P.scale_h, P.scale_l};
     uint32_t phase = 0;
     for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
         // tile base: tile index with zeros inserted at the tile qubits
@@ -342,13 +498,13 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
             const uint32_t q = P.tq[p];
             base = ((base >> q) << (q + 1)) | (base & ((1ull << q) - 1ull));
         }
-        if (tid < 32) {
+        if (tid < lanes) {
             if (tid == 0) {
                 fence_proxy_async();
                 mbar_arrive_expect_tx(&mbar, (1u << P.k) * 16u);
             }
-            __syncwarp(nthr >= 32 ? 0xffffffffu : ((1u << nthr) - 1u));
-            for (uint32_t s = tid; s < nseg; s += 32)
+            __syncwarp(lanes == 32 ? 0xffffffffu : ((1u << lanes) - 1u));
+            for (uint32_t s = tid; s < nseg; s += lanes)
                 tma_load_1d(tile + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 16u, &mbar);
         }
         uint32_t it = 0;
@@ -372,44 +528,87 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
             const DStage& S = P.stages[si];
             uint32_t tl = 0;
 #pragma unroll
-            for (int i = 0; i < kTileQ - kRegQ; ++i)
-                if (i < (int)(P.k - kRegQ) && ((tid >> i) & 1u)) tl |= 1u << S.tbit[i];
-            uint32_t roff[kRegQ];
+            for (int i = 0; i < NTB; ++i)
+                if (i < (int)(P.k - KR) && ((tid >> i) & 1u)) tl |= 1u << S.tbit[i];
+            uint32_t roff[KR];
 #pragma unroll
-            for (int b = 0; b < kRegQ; ++b) roff[b] = 1u << S.rbit[b];
-            dfc v[kSlots];
+            for (int b = 0; b < KR; ++b) roff[b] = 1u << S.rbit[b];
+            dfc v[SLOTS];
 #pragma unroll
-            for (int j = 0; j < kSlots; ++j) {
+            for (int j = 0; j < SLOTS; ++j) {
                 uint32_t l = tl;
 #pragma unroll
-                for (int b = 0; b < kRegQ; ++b)
+                for (int b = 0; b < KR; ++b)
                     if (j & (1 << b)) l += roff[b];
                 const float4 a = tile[l];
                 v[j].re = df{a.x, a.y};
                 v[j].im = df{a.z, a.w};
             }
-            for (uint32_t gi = S.gbegin; gi < S.gend; ++gi) apply_gate(v, P, P.gates[gi], tid, base);
+            for (uint32_t gi = S.gbegin; gi < S.gend; ++gi) apply_gate<KR>(v, P, P.gates[gi], tid, base);
+            const bool last_scaled = P.has_scale && si + 1 == P.nstages;
 #pragma unroll
-            for (int j = 0; j < kSlots; ++j) {
+            for (int j = 0; j < SLOTS; ++j) {
                 uint32_t l = tl;
 #pragma unroll
-                for (int b = 0; b < kRegQ; ++b)
+                for (int b = 0; b < KR; ++b)
                     if (j & (1 << b)) l += roff[b];
-                tile[l] = make_float4(v[j].re.h, v[j].re.l, v[j].im.h, v[j].im.l);
+                df re = v[j].re, im = v[j].im;
+                if (last_scaled) {
+                    re = df_mul_raw(scale, re);
+                    im = df_mul_raw(scale, im);
+                }
+                re = df_renorm(re);
+                im = df_renorm(im);
+                tile[l] = make_float4(re.h, re.l, im.h, im.l);
             }
             __syncthreads();
         }
         fence_proxy_async();
         __syncthreads();
-        if (tid < 32) {
-            for (uint32_t s = tid; s < nseg; s += 32)
+        if (tid < lanes) {
+            for (uint32_t s = tid; s < nseg; s += lanes)
                 tma_store_1d(psi + (base | seg_off[s]), tile + (size_t)s * seg_amps, seg_amps * 16u);
             bulk_commit();
             bulk_wait_read0();
         }
         __syncthreads();
     }
-    if (tid < 32) bulk_wait0();
+    if (tid < lanes) bulk_wait0();
+}
+
+// ---- kernel configurations ----------------------------------------------------------------------
+using KernelFn = void (*)(float4*, PassParams, int*);
+
+struct KCfg {
+    int kt, kr, minb;
+    KernelFn fn;
+};
+
+const KCfg kCfgs[] = {
+    {12, 4, 2, fused_df_kernel<12, 4, 2>},  // 256 threads x 16 amplitudes, 64 KB tile
+    {11, 3, 4, fused_df_kernel<11, 3, 4>},  // 256 threads x 8 amplitudes, 32 KB tile
+    {12, 3, 2, fused_df_kernel<12, 3, 2>},  // 512 threads x 8 amplitudes, 64 KB tile
+    {12, 4, 1, fused_df_kernel<12, 4, 1>},  // 256 threads x 16 amplitudes, up to 255 registers
+};
+
+void launch_cfg(size_t ci, unsigned grid, unsigned block, size_t smem, cudaStream_t s, float4* psi,
+                const PassParams& P, int* err) {
+    switch (ci) {
+    case 1: fused_df_kernel<11, 3, 4><<<grid, block, smem, s>>>(psi, P, err); break;
+    case 2: fused_df_kernel<12, 3, 2><<<grid, block, smem, s>>>(psi, P, err); break;
+    case 3: fused_df_kernel<12, 4, 1><<<grid, block, smem, s>>>(psi, P, err); break;
+    default: fused_df_kernel<12, 4, 2><<<grid, block, smem, s>>>(psi, P, err); break;
+    }
+}
+
+const KCfg& active_cfg() {
+    static int idx = [] {
+        const char* e = std::getenv("QVNT_FUSED_CFG");
+        if (!e) return 0;
+        int i = std::atoi(e);
+        return (i >= 0 && i < (int)(sizeof(kCfgs) / sizeof(kCfgs[0]))) ? i : 0;
+    }();
+    return kCfgs[idx];
 }
 
 // ---- host: lowering qvnt gates to engine gates ----------------------------------------------------
@@ -417,15 +616,22 @@ struct C2 {
     double re, im;
 };
 
+C2 cmul(C2 a, C2 b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+C2 cadd(C2 a, C2 b) { return {a.re + b.re, a.im + b.im}; }
+
 struct EGate {
     uint8_t op = 0;
     uint8_t form0 = F_ID, form1 = F_ID;
     uint8_t dkind = D_PAR;
     bool exact = false;
-    int q0 = -1, q1 = -1;   // target qubits (q0 < q1 for two-qubit ops)
+    bool hadd = false;    // unscaled Hadamard butterfly: contributes 1/sqrt(2) to the pass scale
+    bool one0 = false;    // diagonal: table entry 0 is exactly 1
+    bool has_m2 = false;  // one-qubit gate with its 2x2 matrix in m2 (mergeable)
+    int q0 = -1, q1 = -1;  // target qubits (q0 < q1 for two-qubit ops)
     uint64_t ctrl = 0;
     uint64_t dmask = 0;
     uint32_t codes = 0;
+    C2 m2[4];
     std::vector<float> coef;  // df64 pairs
     int cost = 0;             // FP32 instructions per amplitude (estimate)
     bool standalone = false;
@@ -440,21 +646,24 @@ void push_df(std::vector<float>& out, double x) {
 
 inline unsigned popc(uint64_t x) { return (unsigned)__builtin_popcountll(x); }
 
+const C2 kI4[4] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};  // i^k
+
 // i^code for the exact phases.
 int exact_code(C2 z) {
-    if (z.re == 1.0 && z.im == 0.0) return 0;
-    if (z.re == 0.0 && z.im == 1.0) return 1;
-    if (z.re == -1.0 && z.im == 0.0) return 2;
-    if (z.re == 0.0 && z.im == -1.0) return 3;
+    for (int k = 0; k < 4; ++k)
+        if (z.re == kI4[k].re && z.im == kI4[k].im) return k;
     return -1;
 }
 
 int form_cost(uint8_t f) {
     switch (f) {
     case F_ID: return 0;
-    case F_PERM: return 4;
-    case F_RX: case F_REAL: return 40;
-    default: return 85;
+    case F_SWAPX: return 1;
+    case F_PY: case F_PI: case F_PMI: return 3;
+    case F_PERM: return 6;
+    case F_HADD: return 18;
+    case F_RX: case F_REAL: return 36;
+    default: return 76;
     }
 }
 
@@ -478,32 +687,72 @@ EGate diag_gate(uint64_t mask, uint64_t ctrl, const std::vector<C2>& table, uint
             push_df(e.coef, z.re);
             push_df(e.coef, z.im);
         }
-    e.cost = exact ? 8 : 42;
+    const bool one0 = table[0].re == 1.0 && table[0].im == 0.0;
+    e.one0 = one0;
+    if (popc(mask) == 1 && dkind == D_PAR) e.cost = exact ? 3 : (one0 ? 18 : 34);
+    else e.cost = exact ? 8 : 38;
+    if (popc(mask) == 1 && dkind == D_PAR) {
+        e.has_m2 = true;
+        e.q0 = __builtin_ctzll(mask);
+        e.m2[0] = table[0];
+        e.m2[1] = {0, 0};
+        e.m2[2] = {0, 0};
+        e.m2[3] = table[1];
+    }
     return e;
 }
 
-EGate g1_gate(int q, uint64_t ctrl, uint8_t form, double a, double b, double c, double d) {
+// One-qubit gate with the given 2x2 matrix, in the cheapest form that represents it.
+EGate g1_matrix(int q, uint64_t ctrl, const C2* m) {
     EGate e;
     e.op = OP_G1;
     e.q0 = q;
     e.ctrl = ctrl;
-    e.form0 = form;
-    push_df(e.coef, a);
-    push_df(e.coef, b);
-    push_df(e.coef, c);
-    push_df(e.coef, d);
-    e.cost = form_cost(form);
+    e.has_m2 = true;
+    for (int k = 0; k < 4; ++k) e.m2[k] = m[k];
+    const bool real = m[0].im == 0 && m[1].im == 0 && m[2].im == 0 && m[3].im == 0;
+    const bool rx = m[0].im == 0 && m[3].im == 0 && m[1].re == 0 && m[2].re == 0;
+    const int c01 = exact_code(m[1]), c10 = exact_code(m[2]);
+    const bool anti = m[0].re == 0 && m[0].im == 0 && m[3].re == 0 && m[3].im == 0;
+    // exact anti-diagonal forms: [[0,1],[1,0]], [[0,-i],[i,0]], [[0,i],[i,0]], [[0,-i],[-i,0]]
+    uint8_t perm_form = F_ID;
+    if (anti && c01 == 0 && c10 == 0) perm_form = F_SWAPX;
+    else if (anti && c01 == 3 && c10 == 1) perm_form = F_PY;
+    else if (anti && c01 == 1 && c10 == 1) perm_form = F_PI;
+    else if (anti && c01 == 3 && c10 == 3) perm_form = F_PMI;
+    if (perm_form != F_ID) {
+        e.form0 = perm_form;
+        e.codes = (uint32_t)c01 | ((uint32_t)c10 << 4);
+    } else if (real) {
+        e.form0 = F_REAL;
+        push_df(e.coef, m[0].re);
+        push_df(e.coef, m[1].re);
+        push_df(e.coef, m[2].re);
+        push_df(e.coef, m[3].re);
+    } else if (rx) {
+        e.form0 = F_RX;
+        push_df(e.coef, m[0].re);
+        push_df(e.coef, m[1].im);
+        push_df(e.coef, m[2].im);
+        push_df(e.coef, m[3].re);
+    } else {
+        e.form0 = F_GEN;
+        for (int k = 0; k < 4; ++k) {
+            push_df(e.coef, m[k].re);
+            push_df(e.coef, m[k].im);
+        }
+    }
+    e.cost = form_cost(e.form0);
     return e;
 }
 
-EGate g1_perm(int q, uint64_t ctrl, int c01, int c10) {
+EGate g1_hadd(int q) {
     EGate e;
     e.op = OP_G1;
     e.q0 = q;
-    e.ctrl = ctrl;
-    e.form0 = F_PERM;
-    e.codes = (uint32_t)c01 | ((uint32_t)c10 << 4);
-    e.cost = 4;
+    e.form0 = F_HADD;
+    e.hadd = true;
+    e.cost = form_cost(F_HADD);
     return e;
 }
 
@@ -518,8 +767,8 @@ void push_block(EGate& e, uint8_t form, const C2* m) {  // m: row-major 2x2
         for (int k = 0; k < 8; ++k) e.coef.push_back(0.f);  // blocks are 16 floats apart
     } else {
         for (int k = 0; k < 4; ++k) {
-            push_df(e.coef, m[k].re);
-            push_df(e.coef, m[k].im);
+            push_df(e.coef, m ? m[k].re : 0.0);
+            push_df(e.coef, m ? m[k].im : 0.0);
         }
     }
 }
@@ -535,9 +784,8 @@ EGate g2p_gate(uint64_t ab, uint64_t ctrl, uint8_t fa, const C2* ma, uint32_t co
     e.form0 = fa;
     e.form1 = fb;
     e.codes = codes_a | (codes_b << 8);
-    const C2 zero[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
-    push_block(e, fa == F_PERM || fa == F_ID ? F_GEN : fa, fa == F_PERM || fa == F_ID ? zero : ma);
-    push_block(e, fb == F_PERM || fb == F_ID ? F_GEN : fb, fb == F_PERM || fb == F_ID ? zero : mb);
+    push_block(e, fa == F_RX || fa == F_REAL || fa == F_GEN ? fa : F_GEN, fa == F_RX || fa == F_REAL || fa == F_GEN ? ma : nullptr);
+    push_block(e, fb == F_RX || fb == F_REAL || fb == F_GEN ? fb : F_GEN, fb == F_RX || fb == F_REAL || fb == F_GEN ? mb : nullptr);
     e.cost = (form_cost(fa) + form_cost(fb) + 1) / 2 + 2;
     return e;
 }
@@ -555,32 +803,34 @@ void lower(const qvnt_gate& g, size_t src, std::vector<EGate>& out) {
     switch (g.kind) {
     case QVNT_GATE_ID:
         return;
-    case QVNT_GATE_X:  // x.rs: a product of single-bit flips (exact)
-        each_bit(a, [&](int q) { out.push_back(g1_perm(q, ctrl, 0, 0)); });
+    case QVNT_GATE_X: {  // x.rs: a product of single-bit flips (exact)
+        const C2 m[4] = {{0, 0}, {1, 0}, {1, 0}, {0, 0}};
+        each_bit(a, [&](int q) { out.push_back(g1_matrix(q, ctrl, m)); });
         return;
-    case QVNT_GATE_Y:  // y.rs: Y(mask) = tensor product of single-qubit Y = [[0, -i], [i, 0]] (exact)
-        each_bit(a, [&](int q) { out.push_back(g1_perm(q, ctrl, 3, 1)); });
+    }
+    case QVNT_GATE_Y: {  // y.rs: Y(mask) = tensor product of single-qubit Y = [[0, -i], [i, 0]] (exact)
+        const C2 m[4] = {{0, 0}, {0, -1}, {0, 1}, {0, 0}};
+        each_bit(a, [&](int q) { out.push_back(g1_matrix(q, ctrl, m)); });
         return;
+    }
     case QVNT_GATE_Z:  // z.rs: sign by parity
         if (a) out.push_back(diag_gate(a, ctrl, {{1, 0}, {-1, 0}}, D_PAR));
         return;
     case QVNT_GATE_S: {  // s.rs: i^popcount (dagger: i^-popcount)
         if (!a) return;
         std::vector<C2> t;
-        const C2 p4[4] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
         const int n = popc(a) == 1 ? 2 : 8;
-        for (int k = 0; k < n; ++k) t.push_back(p4[(g.dagger ? (8 - k) : k) & 3]);
+        for (int k = 0; k < n; ++k) t.push_back(kI4[(g.dagger ? (8 - k) : k) & 3]);
         out.push_back(diag_gate(a, ctrl, t, n == 2 ? D_PAR : D_POP));
         return;
     }
     case QVNT_GATE_T: {  // t.rs: rotate(count >> 1), times e^{i pi/4} when count is odd
         if (!a) return;
         std::vector<C2> t;
-        const C2 p4[4] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
         const int n = popc(a) == 1 ? 2 : 8;
         for (int k = 0; k < n; ++k) {
             const int kk = g.dagger ? ((8 - k) & 7) : k;
-            C2 z = p4[(kk >> 1) & 3];
+            C2 z = kI4[(kk >> 1) & 3];
             if (kk & 1) z = C2{z.re * r - z.im * r, z.re * r + z.im * r};
             t.push_back(z);
         }
@@ -591,34 +841,27 @@ void lower(const qvnt_gate& g, size_t src, std::vector<EGate>& out) {
     case QVNT_GATE_RZZ:  // rzz.rs: (c, -s) for even parity, (c, s) for odd
         out.push_back(diag_gate(a, ctrl, {{c, -s}, {c, s}}, D_PAR));
         return;
-    case QVNT_GATE_RX:  // rx.rs: c p0 - i s p1
-        out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_RX, c, -s, -s, c));
+    case QVNT_GATE_RX: {  // rx.rs: c p0 - i s p1
+        const C2 m[4] = {{c, 0}, {0, -s}, {0, -s}, {c, 0}};
+        out.push_back(g1_matrix(__builtin_ctzll(a), ctrl, m));
         return;
-    case QVNT_GATE_RY:  // ry.rs: [[c, -s], [s, c]]
-        out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_REAL, c, -s, s, c));
+    }
+    case QVNT_GATE_RY: {  // ry.rs: [[c, -s], [s, c]]
+        const C2 m[4] = {{c, 0}, {-s, 0}, {s, 0}, {c, 0}};
+        out.push_back(g1_matrix(__builtin_ctzll(a), ctrl, m));
         return;
+    }
     case QVNT_GATE_H1:  // h1.rs
-        out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_REAL, r, r, r, -r));
+    case QVNT_GATE_H2: {  // h2.rs = H on each of the two qubits
+        const C2 m[4] = {{r, 0}, {r, 0}, {r, 0}, {-r, 0}};
+        const uint64_t bits = g.kind == QVNT_GATE_H2 ? (g.a_mask | g.b_mask) : a;
+        each_bit(bits, [&](int q) { out.push_back(ctrl ? g1_matrix(q, ctrl, m) : g1_hadd(q)); });
         return;
-    case QVNT_GATE_H2:  // h2.rs = H on each of the two qubits
-        out.push_back(g1_gate(__builtin_ctzll(g.a_mask), ctrl, F_REAL, r, r, r, -r));
-        out.push_back(g1_gate(__builtin_ctzll(g.b_mask), ctrl, F_REAL, r, r, r, -r));
-        return;
+    }
     case QVNT_GATE_U1: {  // u1.rs: dense 2x2
-        const double* m = g.matrix;
-        const bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
-        if (real) {
-            out.push_back(g1_gate(__builtin_ctzll(a), ctrl, F_REAL, m[0], m[2], m[4], m[6]));
-        } else {
-            EGate e;
-            e.op = OP_G1;
-            e.q0 = __builtin_ctzll(a);
-            e.ctrl = ctrl;
-            e.form0 = F_GEN;
-            for (int k = 0; k < 8; ++k) push_df(e.coef, m[k]);
-            e.cost = form_cost(F_GEN);
-            out.push_back(e);
-        }
+        const C2 m[4] = {{g.matrix[0], g.matrix[1]}, {g.matrix[2], g.matrix[3]},
+                         {g.matrix[4], g.matrix[5]}, {g.matrix[6], g.matrix[7]}};
+        out.push_back(g1_matrix(__builtin_ctzll(a), ctrl, m));
         return;
     }
     case QVNT_GATE_RXX: {  // rxx.rs: c p - i s p(partner) on both pairs
@@ -633,11 +876,11 @@ void lower(const qvnt_gate& g, size_t src, std::vector<EGate>& out) {
         return;
     }
     case QVNT_GATE_SWAP:  // swap.rs
-        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, F_PERM, nullptr, 0));
+        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, F_SWAPX, nullptr, 0));
         return;
     case QVNT_GATE_ISWAP: {  // i_swap.rs: i p(partner) (dagger: -i)
         const uint32_t code = g.dagger ? 3u : 1u;
-        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, F_PERM, nullptr, code | (code << 4)));
+        out.push_back(g2p_gate(a, ctrl, F_ID, nullptr, 0, g.dagger ? F_PMI : F_PI, nullptr, code | (code << 4)));
         return;
     }
     case QVNT_GATE_SQRT_SWAP: {  // sqrt_swap.rs: 0.5(1+i) p + 0.5(1-i) p(partner) (dagger: conjugate)
@@ -667,20 +910,53 @@ void lower(const qvnt_gate& g, size_t src, std::vector<EGate>& out) {
         e.q0 = std::min(qa, qb);
         e.q1 = std::max(qa, qb);
         // engine member order: (bit q0) | (bit q1) << 1; swap the roles of a and b when qa > qb
-        auto perm = [&](int r) { return qa < qb ? r : (((r & 1) << 1) | ((r >> 1) & 1)); };
+        auto perm = [&](int rr) { return qa < qb ? rr : (((rr & 1) << 1) | ((rr >> 1) & 1)); };
         for (int rr = 0; rr < 4; ++rr)
             for (int cc = 0; cc < 4; ++cc) {
                 const int sr = perm(rr), sc = perm(cc);
                 push_df(e.coef, g.matrix[2 * (4 * sr + sc)]);
                 push_df(e.coef, g.matrix[2 * (4 * sr + sc) + 1]);
             }
-        e.cost = 170;
+        e.cost = 150;
         out.push_back(e);
         return;
     }
     default:
         return;
     }
+}
+
+// Merges runs of consecutive one-qubit gates on the same qubit and control mask into one 2x2
+// matrix (multiplied in double precision) when that is cheaper than running them one by one.
+void merge_one_qubit_runs(std::vector<EGate>& eg) {
+    std::vector<EGate> out;
+    out.reserve(eg.size());
+    size_t i = 0;
+    while (i < eg.size()) {
+        size_t j = i;
+        if (eg[i].has_m2) {
+            while (j + 1 < eg.size() && eg[j + 1].has_m2 && eg[j + 1].q0 == eg[i].q0 && eg[j + 1].ctrl == eg[i].ctrl) ++j;
+        }
+        int total = 0;
+        for (size_t k = i; k <= j; ++k) total += eg[k].cost;
+        if (j > i && total > form_cost(F_GEN)) {
+            C2 M[4] = {eg[i].m2[0], eg[i].m2[1], eg[i].m2[2], eg[i].m2[3]};
+            for (size_t k = i + 1; k <= j; ++k) {
+                const C2* A = eg[k].m2;  // applied after M: M <- A M
+                C2 R[4];
+                R[0] = cadd(cmul(A[0], M[0]), cmul(A[1], M[2]));
+                R[1] = cadd(cmul(A[0], M[1]), cmul(A[1], M[3]));
+                R[2] = cadd(cmul(A[2], M[0]), cmul(A[3], M[2]));
+                R[3] = cadd(cmul(A[2], M[1]), cmul(A[3], M[3]));
+                for (int w = 0; w < 4; ++w) M[w] = R[w];
+            }
+            out.push_back(g1_matrix(eg[i].q0, eg[i].ctrl, M));
+        } else {
+            for (size_t k = i; k <= j; ++k) out.push_back(eg[k]);
+        }
+        i = j + 1;
+    }
+    eg.swap(out);
 }
 
 uint64_t targets_of(const EGate& e) {
@@ -702,35 +978,34 @@ struct PlannedPass {
     std::vector<size_t> members;  // indices into the engine gate list
 };
 
-// Pass budget in estimated FP32 instructions per amplitude: about what one HBM round trip of the
-// tile hides at full bandwidth (32 B per amplitude at ~6.8 TB/s against ~114 FFMA/clk/SM).
-constexpr int kPassBudget = 220;
+// Pass budget in estimated FP32 instructions per amplitude (form_cost units): about what one HBM
+// round trip of the tile hides (32 B per amplitude at ~6.8 TB/s against ~114 FFMA/clk/SM).
+int pass_budget() {
+    static int b = [] {
+        const char* e = std::getenv("QVNT_PASS_BUDGET");
+        const int v = e ? std::atoi(e) : 0;
+        return v > 0 ? v : 200;
+    }();
+    return b;
+}
 constexpr size_t kLookahead = 2048;
 
-}  // namespace
-
-void FusedState::release() {
-    if (d_buf) cudaFree(d_buf);
-    if (h_buf) cudaFreeHost(h_buf);
-    d_buf = nullptr;
-    h_buf = nullptr;
-    d_bytes = h_bytes = 0;
-}
-
-int plan_fused(const qvnt_gate* gates, size_t count, uint32_t L, uint32_t fusion_k, std::vector<EGate>& eg,
-               std::vector<uint64_t>& tgt, std::vector<PlannedPass>& passes, uint32_t* kk_out) {
-    const uint32_t k = std::min<uint32_t>(fusion_k ? fusion_k : kTileQ, std::min<uint32_t>(L, kTileQ));
-    const uint32_t kk = std::max<uint32_t>(k, kRegQ);
+int plan_fused(const qvnt_gate* gates, size_t count, uint32_t L, uint32_t fusion_k, const KCfg& cfg,
+               std::vector<EGate>& eg, std::vector<uint64_t>& tgt, std::vector<PlannedPass>& passes,
+               uint32_t* kk_out) {
+    const uint32_t k = std::min<uint32_t>(fusion_k ? fusion_k : cfg.kt, std::min<uint32_t>(L, cfg.kt));
+    const uint32_t kk = std::max<uint32_t>(k, cfg.kr);
     // At least two free tile slots, so that every two-qubit gate fits an empty pass.
     const uint32_t c0 = std::min<uint32_t>(kLowQ, kk - 2);
     const uint64_t low = (1ull << c0) - 1ull;
     const uint64_t all = (1ull << L) - 1ull;
+    const int budget_max = pass_budget();
     *kk_out = kk;
 
-    // ---- lower ----
     eg.clear();
     eg.reserve(count * 2);
     for (size_t i = 0; i < count; ++i) lower(gates[i], i, eg);
+    merge_one_qubit_runs(eg);
     const size_t ne = eg.size();
     std::vector<uint64_t> tch(ne);
     tgt.assign(ne, 0);
@@ -740,7 +1015,6 @@ int plan_fused(const qvnt_gate* gates, size_t count, uint32_t L, uint32_t fusion
         tch[i] = eg[i].standalone ? ~0ull : touched_of(eg[i]);
     }
 
-    // ---- plan passes ----
     std::vector<char> done(ne, 0);
     passes.clear();
     size_t first = 0;
@@ -768,7 +1042,7 @@ int plan_fused(const qvnt_gate* gates, size_t count, uint32_t L, uint32_t fusion
             const bool diag = g.op == OP_DIAG;
             const bool conflict = diag ? (tch[j] & block_nd) != 0 : (tch[j] & (block_nd | block_d)) != 0;
             bool take = false;
-            if (!conflict && !g.standalone && budget + g.cost <= kPassBudget && p.members.size() < (size_t)kMaxGates &&
+            if (!conflict && !g.standalone && budget + g.cost <= budget_max && p.members.size() < (size_t)kMaxGates &&
                 ncoef + g.coef.size() <= (size_t)kMaxCoef) {
                 const uint64_t need = tgt[j] & ~Q;
                 if (popc(need) <= free_slots) {
@@ -787,31 +1061,57 @@ int plan_fused(const qvnt_gate* gates, size_t count, uint32_t L, uint32_t fusion
             if (diag) block_d |= tch[j];
             else block_nd |= tch[j];
             if ((block_nd & all) == all) break;
-            if (budget >= kPassBudget) break;
+            if (budget >= budget_max) break;
         }
+        if (p.members.empty())
+            return set_error(QVNT_ERR_UNSUPPORTED, "fused planner could not place engine gate %zu", first);
         for (uint32_t b = 0; b < L && free_slots > 0; ++b)
             if (!((Q >> b) & 1ull)) {
                 Q |= 1ull << b;
                 --free_slots;
             }
-        if (p.members.empty())
-            return set_error(QVNT_ERR_UNSUPPORTED, "fused planner could not place engine gate %zu", first);
         p.qmask = Q;
         passes.push_back(p);
     }
     return QVNT_OK;
 }
 
+// Register stages of a pass: contiguous runs of members whose targets fit kr register bits.
+template <class LocalFn>
+void build_stages(const PlannedPass& p, const std::vector<EGate>& eg, const std::vector<uint64_t>& tgt, int kr,
+                  LocalFn&& local, std::vector<std::pair<uint32_t, std::vector<size_t>>>& stages) {
+    stages.clear();
+    for (size_t m : p.members) {
+        const uint32_t lt = local(tgt[m]);
+        if (stages.empty() || (eg[m].op != OP_DIAG && popc(stages.back().first | lt) > (unsigned)kr))
+            stages.push_back({lt, {}});
+        else
+            stages.back().first |= lt;
+        stages.back().second.push_back(m);
+    }
+}
+
 template <class F>
 int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>& eg, const std::vector<uint64_t>& tgt,
-                  const std::vector<PlannedPass>& passes, uint32_t kk, F&& standalone_gate) {
+                  const std::vector<PlannedPass>& passes, uint32_t kk, const KCfg& cfg, F&& standalone_gate) {
     const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
+    const int kr = cfg.kr;
     PassParams* P = new PassParams;
     int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
     const size_t smem = ((size_t)1 << kk) * 16;
-    if (smem > 48 * 1024)
-        QVNT_CUDA_TRY(cudaFuncSetAttribute(fused_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static bool attr_set[sizeof(kCfgs) / sizeof(kCfgs[0])] = {};
+    const size_t ci = (size_t)(&cfg - kCfgs);
+    if (!attr_set[ci]) {
+        QVNT_CUDA_TRY(cudaFuncSetAttribute((const void*)cfg.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(((size_t)1 << cfg.kt) * 16)));
+        attr_set[ci] = true;
+    }
+    int per_sm = 0;
+    QVNT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)cfg.fn,
+                                                                1 << (cfg.kt - cfg.kr), smem));
+    if (per_sm < 1) per_sm = 1;
     int status = QVNT_OK;
+    std::vector<std::pair<uint32_t, std::vector<size_t>>> stages;
     for (const PlannedPass& p : passes) {
         if (p.standalone) {
             status = standalone_gate(gates[p.src]);
@@ -830,7 +1130,7 @@ int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>&
         while (run < n && P->tq[run] == run) ++run;
         P->k = n;
         P->c = std::min<uint32_t>(run, n);
-        P->nthreads = 1u << (n - kRegQ);
+        P->nthreads = 1u << (n - kr);
         P->ntiles = r->len >> n;
         auto local = [&](uint64_t m) {  // global mask (within Q) -> tile-local mask
             uint32_t lm = 0;
@@ -838,30 +1138,46 @@ int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>&
                 if (((m & p.qmask) >> b) & 1ull) lm |= 1u << pos_of[b];
             return lm;
         };
-        // stages: contiguous runs of members whose targets fit 4 register bits
-        std::vector<std::pair<uint32_t, std::vector<size_t>>> stages;  // (register local mask, gates)
-        for (size_t m : p.members) {
-            const uint32_t lt = local(tgt[m]);
-            if (stages.empty() || (eg[m].op != OP_DIAG && popc(stages.back().first | lt) > (unsigned)kRegQ))
-                stages.push_back({lt, {}});
-            else
-                stages.back().first |= lt;
-            stages.back().second.push_back(m);
-        }
+        build_stages(p, eg, tgt, kr, local, stages);
         if (stages.size() > (size_t)kMaxStages) {
             status = set_error(QVNT_ERR_UNSUPPORTED, "pass needs %zu stages", stages.size());
             break;
+        }
+        // deferred Hadamard scale 2^(-m/2) of the pass, exact as a df pair
+        int m_h = 0;
+        for (size_t m : p.members) m_h += eg[m].hadd ? 1 : 0;
+        if (m_h) {
+            const double pw = std::ldexp(1.0, -(m_h / 2));
+            if (m_h & 1) {
+                const double rr = 0.70710678118654752440084436210484903;
+                const float h = (float)rr;
+                P->scale_h = (float)((double)h * pw);
+                P->scale_l = (float)((rr - (double)h) * pw);
+            } else {
+                P->scale_h = (float)pw;
+                P->scale_l = 0.f;
+            }
+            P->has_scale = 1;
         }
         P->nstages = (uint32_t)stages.size();
         uint32_t ng = 0, nc = 0;
         for (size_t si = 0; si < stages.size(); ++si) {
             uint32_t R = stages[si].first;
-            // fill the register bits with the highest free tile bits (keeps lanes on low tile bits)
-            for (int b = (int)n - 1; b >= 0 && popc(R) < (unsigned)kRegQ; --b)
+            // Fill the free register bits, preferring qubits that single-qubit diagonals and controls
+            // of this stage read (their slot selection then folds at compile time), then the highest
+            // free tile bits (keeps the lanes on low tile bits).
+            auto add_pref = [&](uint32_t bits) {
+                for (uint32_t b = 0; b < n && popc(R) < (unsigned)kr; ++b)
+                    if (((bits >> b) & 1u) && !((R >> b) & 1u)) R |= 1u << b;
+            };
+            for (size_t m : stages[si].second)
+                if (eg[m].op == OP_DIAG && popc(eg[m].dmask) == 1) add_pref(local(eg[m].dmask));
+            for (size_t m : stages[si].second) add_pref(local(eg[m].ctrl));
+            for (int b = (int)n - 1; b >= 0 && popc(R) < (unsigned)kr; --b)
                 if (!((R >> b) & 1u)) R |= 1u << b;
             DStage& S = P->stages[si];
             uint32_t nb = 0, nt = 0;
-            uint32_t rix[kTileQ], tix[kTileQ];
+            uint32_t rix[kMaxKT], tix[kMaxKT];
             for (uint32_t b = 0; b < n; ++b) {
                 if ((R >> b) & 1u) {
                     rix[b] = nb;
@@ -904,35 +1220,24 @@ int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>&
                         }
                     G.dm_reg = (uint8_t)dreg;
                     G.dm_thr = (uint16_t)dthr;
+                    if (popc(e.dmask) == 1 && e.dkind == D_PAR) {
+                        G.op = OP_DIAG1;
+                        G.one0 = e.one0 ? 1 : 0;
+                        if (dreg) G.b0 = (uint8_t)__builtin_ctz(dreg);
+                    }
                 } else {
                     G.b0 = (uint8_t)rix[pos_of[e.q0]];
                     if (e.q1 >= 0) G.b1 = (uint8_t)rix[pos_of[e.q1]];
-                    if (e.q1 >= 0 && G.b0 > G.b1) {
-                        // register order differs from qubit order: only symmetric blocks reach here for
-                        // G2P; G4 matrices are permuted to register order
-                        std::swap(G.b0, G.b1);
-                        if (e.op == OP_G4) {
-                            float tmp[64];
-                            memcpy(tmp, &P->coef[G.coef], sizeof tmp);
-                            auto perm = [](int x) { return ((x & 1) << 1) | ((x >> 1) & 1); };
-                            for (int rr = 0; rr < 4; ++rr)
-                                for (int cc = 0; cc < 4; ++cc)
-                                    for (int w = 0; w < 4; ++w)
-                                        P->coef[G.coef + 16 * rr + 4 * cc + w] = tmp[16 * perm(rr) + 4 * perm(cc) + w];
-                        }
-                    }
                 }
             }
             S.gend = (uint16_t)ng;
         }
-        const int per_sm = 2;
         uint64_t grid = (uint64_t)r->ctx->geo.sms * per_sm;
         if (grid > P->ntiles) grid = P->ntiles;
         cudaEvent_t stop = nullptr;
         status = timing_begin(r, &stop);
         if (status) break;
-        fused_df_kernel<<<(unsigned)grid, P->nthreads, smem, r->stream>>>(reinterpret_cast<float4*>(r->psi), *P,
-                                                                          d_err);
+        launch_cfg(ci, (unsigned)grid, P->nthreads, smem, r->stream, reinterpret_cast<float4*>(r->psi), *P, d_err);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             status = set_cuda_error(e, "fused_df_kernel launch");
@@ -946,10 +1251,23 @@ int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>&
     delete P;
     return status;
 }
+
+}  // namespace
+
+void FusedState::release() {
+    if (d_buf) cudaFree(d_buf);
+    if (h_buf) cudaFreeHost(h_buf);
+    d_buf = nullptr;
+    h_buf = nullptr;
+    d_bytes = h_bytes = 0;
+}
+
 int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
     const int fmt = FMT_DF64;
-    // Registers below 4 qubits of index space run per-gate passes.
+    const KCfg& cfg = active_cfg();
+    // Gates the tiles do not take, and every gate of registers smaller than a register stage, run
+    // as per-gate passes on the double-float storage.
     auto standalone_gate = [&](const qvnt_gate& g) -> int {
         DevGate d = decode_gate(g);
         if (plain_gate_is_identity(d)) return QVNT_OK;
@@ -966,7 +1284,7 @@ int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
         r->passes += 1;
         return st;
     };
-    if (L < (uint32_t)kRegQ) {
+    if (L < (uint32_t)cfg.kr) {
         for (size_t i = 0; i < count; ++i) {
             int st = standalone_gate(gates[i]);
             if (st) return st;
@@ -974,14 +1292,13 @@ int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
         return QVNT_OK;
     }
     std::vector<EGate> eg;
-    std::vector<uint64_t> tgt, tch;
+    std::vector<uint64_t> tgt;
     std::vector<PlannedPass> passes;
     uint32_t kk = 0;
-    int status = plan_fused(gates, count, L, r->fusion_k, eg, tgt, passes, &kk);
+    int status = plan_fused(gates, count, L, r->fusion_k, cfg, eg, tgt, passes, &kk);
     if (status) return status;
-    return launch_passes(r, gates, eg, tgt, passes, kk, standalone_gate);
+    return launch_passes(r, gates, eg, tgt, passes, kk, cfg, standalone_gate);
 }
-
 
 }  // namespace qvnt
 
@@ -997,32 +1314,33 @@ extern "C" int qvnt_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_n
         if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
     }
     const uint32_t L = (uint32_t)__builtin_ctzll(len);
+    const KCfg& cfg = active_cfg();
     uint64_t np = 0, ns = 0, nq = 0;
-    if (L < (uint32_t)kRegQ) {
+    if (L < (uint32_t)cfg.kr) {
         np = count;
     } else {
         std::vector<EGate> eg;
         std::vector<uint64_t> tgt;
         std::vector<PlannedPass> pl;
         uint32_t kk = 0;
-        int st = plan_fused(gates, count, L, fusion_k, eg, tgt, pl, &kk);
+        int st = plan_fused(gates, count, L, fusion_k, cfg, eg, tgt, pl, &kk);
         if (st) return st;
         np = pl.size();
         nq = eg.size();
+        std::vector<std::pair<uint32_t, std::vector<size_t>>> stg;
         for (const PlannedPass& p : pl) {
             if (p.standalone) continue;
-            // same grouping as launch_passes: a stage holds gates whose targets fit 4 register bits
-            uint64_t cur = 0;
-            bool open = false;
-            for (size_t m : p.members) {
-                if (!open || (eg[m].op != OP_DIAG && __builtin_popcountll(cur | tgt[m]) > kRegQ)) {
-                    ++ns;
-                    open = true;
-                    cur = tgt[m];
-                } else {
-                    cur |= tgt[m];
-                }
-            }
+            auto local = [&](uint64_t m) {  // global mask within the tile -> tile-local mask
+                uint32_t lm = 0, n = 0;
+                for (uint32_t b = 0; b < L; ++b)
+                    if ((p.qmask >> b) & 1ull) {
+                        if ((m >> b) & 1ull) lm |= 1u << n;
+                        ++n;
+                    }
+                return lm;
+            };
+            build_stages(p, eg, tgt, cfg.kr, local, stg);
+            ns += stg.size();
         }
     }
     if (passes) *passes = np;
@@ -1030,7 +1348,3 @@ extern "C" int qvnt_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_n
     if (engine_gates) *engine_gates = nq;
     return QVNT_OK;
 }
-
-namespace qvnt {
-
-}  // namespace qvnt
