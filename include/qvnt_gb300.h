@@ -234,6 +234,26 @@ int qvnt_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint32_
                    uint64_t* stages, uint64_t* engine_gates);
 
 /* ---------------------------------------------------------------------------------------------
+ * Allocation-free norm.  No counterpart in the reference: an extra entry point for callers that
+ * cannot call cudaMalloc -- hosts whose device memory is owned by their own allocator or pool (a
+ * framework's caching allocator, a serving process with a fixed memory budget), and code paths
+ * where cudaMalloc/cudaFree would synchronise the device in the middle of their stream work.
+ *
+ * Sum of |psi_i|^2 over a state vector the caller keeps in device memory: d_psi holds len
+ * interleaved (re, im) IEEE f64 amplitudes; the sum is written to the device double *d_out.  The
+ * kernels are queued on `stream` (a cudaStream_t; NULL = the legacy default stream) and the call
+ * returns without waiting.  It allocates nothing: its partial sums live in a file-scope device
+ * array of QVNT_NOALLOC_MAX_AMPLITUDES / 4096 doubles (512 KiB) that every GPU loading the library
+ * holds until the process exits; len above QVNT_NOALLOC_MAX_AMPLITUDES (2^28, a 28-qubit state) is
+ * rejected with QVNT_ERR_BAD_ARG.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call before any stream
+ * capture.  All calls on a device share the array: calls that overlap on the GPU (different
+ * streams, no ordering between them) race on it.  Same reduction order as qvnt_reg_get_absolute.
+ * ------------------------------------------------------------------------------------------- */
+#define QVNT_NOALLOC_MAX_AMPLITUDES (1ull << 28)
+int qvnt_norm_sqr_noalloc(const double* d_psi, uint64_t len, double* d_out, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Counters for measurement: kernels launched and fused passes run by this register so far.
  * ------------------------------------------------------------------------------------------- */
 int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* passes);

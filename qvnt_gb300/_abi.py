@@ -97,6 +97,7 @@ _PROTOS = {
     "qvnt_ops_dgr": (c_int, [P(QvntGate), c_size]),
     "qvnt_ops_c": (c_int, [P(QvntGate), c_size, c_u64]),
     "qvnt_plan_info": (c_int, [P(QvntGate), c_size, c_u32, c_u32, P(c_u64), P(c_u64), P(c_u64)]),
+    "qvnt_norm_sqr_noalloc": (c_int, [c_void, c_u64, c_void, c_void]),
     "qvnt_reg_stats": (c_int, [c_void, P(c_u64), P(c_u64)]),
     "qvnt_reg_kernel_timing": (c_int, [c_void, c_int, P(c_double), P(c_u64)]),
 }

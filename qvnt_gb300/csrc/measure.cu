@@ -8,6 +8,8 @@
 // (chunk partials, then one block): results are reproducible run to run.
 #include <math.h>
 
+#include <mutex>
+
 #include "atomic.cuh"
 #include "df64.cuh"
 #include "kernels.h"
@@ -410,4 +412,52 @@ int launch_convert(double2* psi, uint64_t len, int to_df, cudaStream_t stream) {
     return QVNT_OK;
 }
 
+// ---- allocation-free norm: scratch in a file-scope device array ---------------------------------
+// Chunk partial sums of qvnt_norm_sqr_noalloc.  Every GPU that loads the library holds this array
+// (512 KiB) until the process exits; all calls on a device share it.
+constexpr uint64_t kNoAllocPartials = QVNT_NOALLOC_MAX_AMPLITUDES / kChunk;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
 }  // namespace qvnt
+
+using namespace qvnt;
+
+// For callers that cannot allocate device memory themselves: the partial sums live in
+// g_noalloc_partials.  Host code cannot use the array's name as a device address, so the address
+// is looked up once per device (with that device current) and cached.
+extern "C" int qvnt_norm_sqr_noalloc(const double* d_psi, uint64_t len, double* d_out, void* stream) {
+    if (!d_psi || !d_out) return set_error(QVNT_ERR_BAD_ARG, "null device pointer");
+    if (len == 0) return set_error(QVNT_ERR_BAD_ARG, "empty state");
+    if (len > QVNT_NOALLOC_MAX_AMPLITUDES)
+        return set_error(QVNT_ERR_BAD_ARG, "state of %llu amplitudes exceeds the allocation-free limit of %llu",
+                         (unsigned long long)len, (unsigned long long)QVNT_NOALLOC_MAX_AMPLITUDES);
+    int dev = 0;
+    QVNT_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(QVNT_ERR_BAD_ARG, "device %d out of range", dev);
+    double* partials = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+            if (e != cudaSuccess) return set_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_partials)");
+            g_noalloc_ptr[dev] = static_cast<double*>(p);
+        }
+        partials = g_noalloc_ptr[dev];
+    }
+    // Every chunk writes its own partial and the final block overwrites *d_out, so nothing left
+    // in the array by an earlier call is read: no clearing is needed.
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint64_t nc = chunk_count(len);
+    chunk_sum_kernel<AccF64><<<(unsigned)nc, kRedThreads, 0, s>>>(reinterpret_cast<const double2*>(d_psi), len,
+                                                                   nullptr, partials);
+    final_sum_kernel<<<1, kScanThreads, 0, s>>>(partials, nc, d_out);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
