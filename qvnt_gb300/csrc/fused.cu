@@ -230,10 +230,21 @@ __device__ __forceinline__ void g2p_block(dfc (&v)[SLOTS], const PassParams& P, 
                                           bool blockA, uint32_t o, uint32_t codes) {
     constexpr int M0 = 1 << B0, M1 = 1 << B1;
     const uint32_t creg = G.ctrl_reg;
+    if (creg == 0) {
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j) {
+            if (j & (M0 | M1)) continue;
+            if (blockA)
+                pair_op<FORM>(v[j], v[j | M0 | M1], P, o, codes);
+            else
+                pair_op<FORM>(v[j | M0], v[j | M1], P, o, codes);
+        }
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < SLOTS; ++j) {
         if (j & (M0 | M1)) continue;
-        if (!(tok && (j & creg) == creg)) continue;
+        if ((j & creg) != creg) continue;
         if (blockA)
             pair_op<FORM>(v[j], v[j | M0 | M1], P, o, codes);
         else
@@ -259,8 +270,82 @@ __device__ __forceinline__ void g2p_any(dfc (&v)[SLOTS], const PassParams& P, co
 
 template <int SLOTS, int B0, int B1>
 __device__ __forceinline__ void g2p(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, bool tok) {
+    constexpr int M0 = 1 << B0, M1 = 1 << B1;
+    if (G.form0 == F_RX && G.form1 == F_RX && G.ctrl_reg == 0) {
+        // RXX / RYY: both blocks RX-shaped, one loop, both coefficient sets loaded once
+        const uint32_t o = G.coef;
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j) {
+            if (j & (M0 | M1)) continue;
+            pair_op<F_RX>(v[j], v[j | M0 | M1], P, o, 0);
+            pair_op<F_RX>(v[j | M0], v[j | M1], P, o + 16, 0);
+        }
+        return;
+    }
     g2p_any<SLOTS, B0, B1>(v, P, G, tok, true);
     g2p_any<SLOTS, B0, B1>(v, P, G, tok, false);
+}
+
+// Parity diagonal: table entry parity(idx & mask) of two.  The register part of the mask has NR = 0,
+// 1 or 2 bits (B0, B1): their parity per slot is a compile-time constant.  The thread and
+// out-of-tile parts give one parity per thread (tpar): slots whose parity equals tpar take entry 0.
+template <int SLOTS, int NR, int B0, int B1>
+__device__ __forceinline__ int slot_par(int j) {
+    return (NR >= 1 ? ((j >> B0) & 1) : 0) ^ (NR >= 2 ? ((j >> B1) & 1) : 0);
+}
+
+template <int SLOTS, int NR, int B0, int B1, int PAR, int Q>
+__device__ __forceinline__ void rot_par(dfc (&v)[SLOTS], uint32_t creg) {
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j)
+        if (slot_par<SLOTS, NR, B0, B1>(j) == PAR && (j & creg) == creg) v[j] = rotc<Q>(v[j]);
+}
+
+template <int SLOTS, int NR, int B0, int B1, int PAR>
+__device__ __forceinline__ void rot_par_code(dfc (&v)[SLOTS], uint32_t creg, uint32_t code) {
+    switch (code & 3u) {
+    case 1: rot_par<SLOTS, NR, B0, B1, PAR, 1>(v, creg); break;
+    case 2: rot_par<SLOTS, NR, B0, B1, PAR, 2>(v, creg); break;
+    case 3: rot_par<SLOTS, NR, B0, B1, PAR, 3>(v, creg); break;
+    default: break;
+    }
+}
+
+template <int SLOTS, int NR, int B0, int B1, int PAR>
+__device__ __forceinline__ void mul_par(dfc (&v)[SLOTS], uint32_t creg, df cr, df ci) {
+    if (creg == 0) {
+#pragma unroll
+        for (int j = 0; j < SLOTS; ++j)
+            if (slot_par<SLOTS, NR, B0, B1>(j) == PAR) v[j] = dfc_mul(cr, ci, v[j]);
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < SLOTS; ++j)
+        if (slot_par<SLOTS, NR, B0, B1>(j) == PAR && (j & creg) == creg) v[j] = dfc_mul(cr, ci, v[j]);
+}
+
+template <int SLOTS, int NR, int B0, int B1>
+__device__ __forceinline__ void diagp(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, uint32_t tid,
+                                      uint64_t base) {
+    const uint32_t creg = G.ctrl_reg;
+    const uint32_t tpar = (__popc(tid & G.dm_thr) + __popcll(base & G.dm_out)) & 1u;
+    if (G.exact) {
+        const uint32_t e0 = G.codes & 3u, e1 = (G.codes >> 4) & 3u;
+        rot_par_code<SLOTS, NR, B0, B1, 0>(v, creg, tpar ? e1 : e0);
+        rot_par_code<SLOTS, NR, B0, B1, 1>(v, creg, tpar ? e0 : e1);
+        return;
+    }
+    const uint32_t o = G.coef;
+    if (G.one0) {
+        // entry 0 is 1: only the slots of odd overall parity change
+        const df r1 = cdf(P, o + 4), i1 = cdf(P, o + 6);
+        if (tpar) mul_par<SLOTS, NR, B0, B1, 0>(v, creg, r1, i1);
+        else mul_par<SLOTS, NR, B0, B1, 1>(v, creg, r1, i1);
+        return;
+    }
+    const uint32_t oa = o + (tpar ? 4u : 0u), ob = o + (tpar ? 0u : 4u);
+    mul_par<SLOTS, NR, B0, B1, 0>(v, creg, cdf(P, oa), cdf(P, oa + 2));
+    mul_par<SLOTS, NR, B0, B1, 1>(v, creg, cdf(P, ob), cdf(P, ob + 2));
 }
 
 // Dense 4x4 on register bits B0 < B1; member r = (bit B0) | (bit B1) << 1, row-major complex matrix.
@@ -279,17 +364,24 @@ __device__ __forceinline__ void g4(dfc (&v)[SLOTS], const PassParams& P, const D
         for (int c = 0; c < 4; ++c) x[c] = v[s[c]];
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            df tr[8], ti[8];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const df mr = cdf(P, o + 16 * r + 4 * c), mi = cdf(P, o + 16 * r + 4 * c + 2);
-                tr[2 * c] = df_mul_raw(mr, x[c].re);
-                tr[2 * c + 1] = df_mul_raw(df_neg(mi), x[c].im);
-                ti[2 * c] = df_mul_raw(mr, x[c].im);
-                ti[2 * c + 1] = df_mul_raw(mi, x[c].re);
+            // term-by-term accumulation keeps only the running sums live
+            df ar = df_mul_raw(cdf(P, o + 16 * r), x[0].re);
+            df ai = df_mul_raw(cdf(P, o + 16 * r), x[0].im);
+            {
+                const df mi = cdf(P, o + 16 * r + 2);
+                ar = df_add_raw(ar, df_mul_raw(df_neg(mi), x[0].im));
+                ai = df_add_raw(ai, df_mul_raw(mi, x[0].re));
             }
-            v[s[r]].re = df_sum_raw<8>(tr);
-            v[s[r]].im = df_sum_raw<8>(ti);
+#pragma unroll
+            for (int c = 1; c < 4; ++c) {
+                const df mr = cdf(P, o + 16 * r + 4 * c), mi = cdf(P, o + 16 * r + 4 * c + 2);
+                ar = df_add_raw(ar, df_mul_raw(mr, x[c].re));
+                ar = df_add_raw(ar, df_mul_raw(df_neg(mi), x[c].im));
+                ai = df_add_raw(ai, df_mul_raw(mr, x[c].im));
+                ai = df_add_raw(ai, df_mul_raw(mi, x[c].re));
+            }
+            v[s[r]].re = ar;
+            v[s[r]].im = ai;
         }
     }
 }
@@ -328,83 +420,6 @@ __device__ __forceinline__ void gdiag(dfc (&v)[SLOTS], const PassParams& P, cons
     }
 }
 
-// Applies a compile-time power of i to the slots whose register bit B equals VAL (and controls hold).
-template <int SLOTS, int B, int VAL, int Q>
-__device__ __forceinline__ void rot_slots(dfc (&v)[SLOTS], uint32_t creg) {
-#pragma unroll
-    for (int j = 0; j < SLOTS; ++j)
-        if (((j >> B) & 1) == VAL && (j & creg) == creg) v[j] = rotc<Q>(v[j]);
-}
-
-template <int SLOTS, int B, int VAL>
-__device__ __forceinline__ void rot_slots_code(dfc (&v)[SLOTS], uint32_t creg, uint32_t code) {
-    switch (code & 3u) {
-    case 1: rot_slots<SLOTS, B, VAL, 1>(v, creg); break;
-    case 2: rot_slots<SLOTS, B, VAL, 2>(v, creg); break;
-    case 3: rot_slots<SLOTS, B, VAL, 3>(v, creg); break;
-    default: break;
-    }
-}
-
-// One-qubit diagonal on register bit B: entry 1 where the bit is set, entry 0 elsewhere.
-template <int SLOTS, int B>
-__device__ __forceinline__ void diag1_reg(dfc (&v)[SLOTS], const PassParams& P, const DGate& G) {
-    const uint32_t creg = G.ctrl_reg;
-    if (G.exact) {
-        rot_slots_code<SLOTS, B, 1>(v, creg, G.codes >> 4);
-        rot_slots_code<SLOTS, B, 0>(v, creg, G.codes);
-        return;
-    }
-    const uint32_t o = G.coef;
-    const df r1 = cdf(P, o + 4), i1 = cdf(P, o + 6);
-#pragma unroll
-    for (int j = 0; j < SLOTS; ++j)
-        if (((j >> B) & 1) && (j & creg) == creg) v[j] = dfc_mul(r1, i1, v[j]);
-    if (!G.one0) {
-        const df r0 = cdf(P, o), i0 = cdf(P, o + 2);
-#pragma unroll
-        for (int j = 0; j < SLOTS; ++j)
-            if (!((j >> B) & 1) && (j & creg) == creg) v[j] = dfc_mul(r0, i0, v[j]);
-    }
-}
-
-// One-qubit diagonal on a thread bit or a bit outside the tile: one phase for all slots of a thread.
-template <int SLOTS>
-__device__ __forceinline__ void diag1_uniform(dfc (&v)[SLOTS], const PassParams& P, const DGate& G, uint32_t tid,
-                                              uint64_t base) {
-    const uint32_t creg = G.ctrl_reg;
-    const bool bit = (tid & G.dm_thr) != 0 || (base & G.dm_out) != 0;
-    if (G.exact) {
-        // a per-thread switch over compile-time rotations: no per-slot selects
-        switch ((bit ? (G.codes >> 4) : G.codes) & 3u) {
-        case 1:
-#pragma unroll
-            for (int j = 0; j < SLOTS; ++j)
-                if ((j & creg) == creg) v[j] = rotc<1>(v[j]);
-            break;
-        case 2:
-#pragma unroll
-            for (int j = 0; j < SLOTS; ++j)
-                if ((j & creg) == creg) v[j] = rotc<2>(v[j]);
-            break;
-        case 3:
-#pragma unroll
-            for (int j = 0; j < SLOTS; ++j)
-                if ((j & creg) == creg) v[j] = rotc<3>(v[j]);
-            break;
-        default:
-            break;
-        }
-        return;
-    }
-    if (!bit && G.one0) return;
-    const uint32_t o = G.coef + (bit ? 4u : 0u);
-    const df cr = cdf(P, o), ci = cdf(P, o + 2);
-#pragma unroll
-    for (int j = 0; j < SLOTS; ++j)
-        if ((j & creg) == creg) v[j] = dfc_mul(cr, ci, v[j]);
-}
-
 template <int KR>
 __device__ __forceinline__ void apply_gate(dfc (&v)[1 << KR], const PassParams& P, const DGate& G, uint32_t tid,
                                            uint64_t base) {
@@ -423,20 +438,38 @@ __device__ __forceinline__ void apply_gate(dfc (&v)[1 << KR], const PassParams& 
             break;
         }
         break;
-    case OP_DIAG1:
-        if (G.dm_reg) {
+    case OP_DIAG1: {
+        // parity diagonal with at most two register bits (b0 < b1 when two)
+        const int nr = __popc(G.dm_reg);
+        if (nr == 0) {
+            diagp<S, 0, 0, 0>(v, P, G, tid, base);
+        } else if (nr == 1) {
             switch (G.b0) {
-            case 0: diag1_reg<S, 0>(v, P, G); break;
-            case 1: diag1_reg<S, 1>(v, P, G); break;
-            case 2: diag1_reg<S, 2>(v, P, G); break;
+            case 0: diagp<S, 1, 0, 0>(v, P, G, tid, base); break;
+            case 1: diagp<S, 1, 1, 0>(v, P, G, tid, base); break;
+            case 2: diagp<S, 1, 2, 0>(v, P, G, tid, base); break;
             default:
-                if constexpr (KR > 3) diag1_reg<S, 3>(v, P, G);
+                if constexpr (KR > 3) diagp<S, 1, 3, 0>(v, P, G, tid, base);
                 break;
             }
         } else {
-            diag1_uniform<S>(v, P, G, tid, base);
+            switch (G.b0 * 4 + G.b1) {
+            case 1: diagp<S, 2, 0, 1>(v, P, G, tid, base); break;
+            case 2: diagp<S, 2, 0, 2>(v, P, G, tid, base); break;
+            case 6: diagp<S, 2, 1, 2>(v, P, G, tid, base); break;
+            default:
+                if constexpr (KR > 3) {
+                    switch (G.b0 * 4 + G.b1) {
+                    case 3: diagp<S, 2, 0, 3>(v, P, G, tid, base); break;
+                    case 7: diagp<S, 2, 1, 3>(v, P, G, tid, base); break;
+                    default: diagp<S, 2, 2, 3>(v, P, G, tid, base); break;
+                    }
+                }
+                break;
+            }
         }
         break;
+    }
     case OP_G2P:
     case OP_G4: {
         const int pr = G.b0 * 4 + G.b1;
@@ -545,21 +578,35 @@ __global__ void __launch_bounds__(1 << (KT - KR), MINB)
                 v[j].im = df{a.z, a.w};
             }
             for (uint32_t gi = S.gbegin; gi < S.gend; ++gi) apply_gate<KR>(v, P, P.gates[gi], tid, base);
-            const bool last_scaled = P.has_scale && si + 1 == P.nstages;
+            // Intermediate stages hand unnormalised pairs to the next stage; the pass's last stage
+            // applies the deferred Hadamard scale and renormalises before the tile goes to HBM.
+            const bool last = si + 1 == P.nstages;
+            if (last) {
+                const bool scaled = P.has_scale != 0;
 #pragma unroll
-            for (int j = 0; j < SLOTS; ++j) {
-                uint32_t l = tl;
+                for (int j = 0; j < SLOTS; ++j) {
+                    uint32_t l = tl;
 #pragma unroll
-                for (int b = 0; b < KR; ++b)
-                    if (j & (1 << b)) l += roff[b];
-                df re = v[j].re, im = v[j].im;
-                if (last_scaled) {
-                    re = df_mul_raw(scale, re);
-                    im = df_mul_raw(scale, im);
+                    for (int b = 0; b < KR; ++b)
+                        if (j & (1 << b)) l += roff[b];
+                    df re = v[j].re, im = v[j].im;
+                    if (scaled) {
+                        re = df_mul_raw(scale, re);
+                        im = df_mul_raw(scale, im);
+                    }
+                    re = df_renorm(re);
+                    im = df_renorm(im);
+                    tile[l] = make_float4(re.h, re.l, im.h, im.l);
                 }
-                re = df_renorm(re);
-                im = df_renorm(im);
-                tile[l] = make_float4(re.h, re.l, im.h, im.l);
+            } else {
+#pragma unroll
+                for (int j = 0; j < SLOTS; ++j) {
+                    uint32_t l = tl;
+#pragma unroll
+                    for (int b = 0; b < KR; ++b)
+                        if (j & (1 << b)) l += roff[b];
+                    tile[l] = make_float4(v[j].re.h, v[j].re.l, v[j].im.h, v[j].im.l);
+                }
             }
             __syncthreads();
         }
@@ -589,6 +636,7 @@ const KCfg kCfgs[] = {
     {11, 3, 4, fused_df_kernel<11, 3, 4>},  // 256 threads x 8 amplitudes, 32 KB tile
     {12, 3, 2, fused_df_kernel<12, 3, 2>},  // 512 threads x 8 amplitudes, 64 KB tile
     {12, 4, 1, fused_df_kernel<12, 4, 1>},  // 256 threads x 16 amplitudes, up to 255 registers
+    {11, 4, 3, fused_df_kernel<11, 4, 3>},  // 128 threads x 16 amplitudes, 32 KB tile, <= 168 registers
 };
 
 void launch_cfg(size_t ci, unsigned grid, unsigned block, size_t smem, cudaStream_t s, float4* psi,
@@ -597,6 +645,7 @@ void launch_cfg(size_t ci, unsigned grid, unsigned block, size_t smem, cudaStrea
     case 1: fused_df_kernel<11, 3, 4><<<grid, block, smem, s>>>(psi, P, err); break;
     case 2: fused_df_kernel<12, 3, 2><<<grid, block, smem, s>>>(psi, P, err); break;
     case 3: fused_df_kernel<12, 4, 1><<<grid, block, smem, s>>>(psi, P, err); break;
+    case 4: fused_df_kernel<11, 4, 3><<<grid, block, smem, s>>>(psi, P, err); break;
     default: fused_df_kernel<12, 4, 2><<<grid, block, smem, s>>>(psi, P, err); break;
     }
 }
@@ -816,25 +865,14 @@ void lower(const qvnt_gate& g, size_t src, std::vector<EGate>& out) {
     case QVNT_GATE_Z:  // z.rs: sign by parity
         if (a) out.push_back(diag_gate(a, ctrl, {{1, 0}, {-1, 0}}, D_PAR));
         return;
-    case QVNT_GATE_S: {  // s.rs: i^popcount (dagger: i^-popcount)
-        if (!a) return;
-        std::vector<C2> t;
-        const int n = popc(a) == 1 ? 2 : 8;
-        for (int k = 0; k < n; ++k) t.push_back(kI4[(g.dagger ? (8 - k) : k) & 3]);
-        out.push_back(diag_gate(a, ctrl, t, n == 2 ? D_PAR : D_POP));
+    case QVNT_GATE_S: {  // s.rs: i^popcount (dagger: i^-popcount) = product of i^bit over the mask
+        const C2 ph = g.dagger ? C2{0, -1} : C2{0, 1};
+        each_bit(a, [&](int q) { out.push_back(diag_gate(1ull << q, ctrl, {{1, 0}, ph}, D_PAR)); });
         return;
     }
-    case QVNT_GATE_T: {  // t.rs: rotate(count >> 1), times e^{i pi/4} when count is odd
-        if (!a) return;
-        std::vector<C2> t;
-        const int n = popc(a) == 1 ? 2 : 8;
-        for (int k = 0; k < n; ++k) {
-            const int kk = g.dagger ? ((8 - k) & 7) : k;
-            C2 z = kI4[(kk >> 1) & 3];
-            if (kk & 1) z = C2{z.re * r - z.im * r, z.re * r + z.im * r};
-            t.push_back(z);
-        }
-        out.push_back(diag_gate(a, ctrl, t, n == 2 ? D_PAR : D_POP));
+    case QVNT_GATE_T: {  // t.rs: e^{i pi/4 popcount} (dagger: e^{-i pi/4 popcount}) = product over the bits
+        const C2 ph = g.dagger ? C2{r, -r} : C2{r, r};
+        each_bit(a, [&](int q) { out.push_back(diag_gate(1ull << q, ctrl, {{1, 0}, ph}, D_PAR)); });
         return;
     }
     case QVNT_GATE_RZ:   // rz.rs: (c, -s) where the bit is 0, (c, s) where it is 1
@@ -1171,7 +1209,7 @@ int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>&
                     if (((bits >> b) & 1u) && !((R >> b) & 1u)) R |= 1u << b;
             };
             for (size_t m : stages[si].second)
-                if (eg[m].op == OP_DIAG && popc(eg[m].dmask) == 1) add_pref(local(eg[m].dmask));
+                if (eg[m].op == OP_DIAG && popc(eg[m].dmask) <= 2) add_pref(local(eg[m].dmask));
             for (size_t m : stages[si].second) add_pref(local(eg[m].ctrl));
             for (int b = (int)n - 1; b >= 0 && popc(R) < (unsigned)kr; --b)
                 if (!((R >> b) & 1u)) R |= 1u << b;
@@ -1220,10 +1258,12 @@ int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>&
                         }
                     G.dm_reg = (uint8_t)dreg;
                     G.dm_thr = (uint16_t)dthr;
-                    if (popc(e.dmask) == 1 && e.dkind == D_PAR) {
+                    if (e.dkind == D_PAR && popc(dreg) <= 2) {
+                        // parity diagonal with at most two register bits: compile-time slot parity
                         G.op = OP_DIAG1;
                         G.one0 = e.one0 ? 1 : 0;
                         if (dreg) G.b0 = (uint8_t)__builtin_ctz(dreg);
+                        if (popc(dreg) == 2) G.b1 = (uint8_t)(31 - __builtin_clz(dreg));
                     }
                 } else {
                     G.b0 = (uint8_t)rix[pos_of[e.q0]];
