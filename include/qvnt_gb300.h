@@ -43,7 +43,8 @@ enum qvnt_status {
     QVNT_ERR_CUDA = 4,        /* CUDA runtime error (message in qvnt_last_error)             */
     QVNT_ERR_TIMEOUT = 5,     /* a bounded device wait ran out                               */
     QVNT_ERR_BAD_ARG = 6,     /* other invalid argument (null pointer, bad kind, size)       */
-    QVNT_ERR_UNSUPPORTED = 7  /* operation not supported by the engine                       */
+    QVNT_ERR_UNSUPPORTED = 7, /* operation not supported by the engine                       */
+    QVNT_ERR_BUSY = 8         /* serving: the admission queue is full, the request was shed   */
 };
 
 /* ---------------------------------------------------------------------------------------------
@@ -261,6 +262,109 @@ int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* pas
  * the fused-pass kernel on the register's stream since the last reset (enable != 0 turns
  * recording on and clears the totals).  *ms = summed event time, *launches = number of launches. */
 int qvnt_reg_kernel_timing(qvnt_reg* reg, int enable, double* ms, uint64_t* launches);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batching form: many independent registers in one persistent launch.  Each register behaves as
+ * `QReg::with_state(q_nums[i], states[i])` (src/register/quant.rs:113-150) followed by `apply` of its
+ * own gate list (quant.rs:376-395) and, when measure_masks[i] != 0, `measure_mask(measure_masks[i])`
+ * (quant.rs:490-501, collapse without renormalisation).  The replacement for a caller looping over
+ * registers on the host; qvnt itself has no batch object.
+ *
+ *   qvnt_batch_create   copies the circuits (gate_offsets[i]..gate_offsets[i+1] of `gates` belong to
+ *                       register i; count + 1 offsets), validates every gate against its register,
+ *                       allocates the states (double-float, 16 B per amplitude), plans the schedule
+ *                       and captures one run as a CUDA graph.  4 <= q_nums[i] <= 26.  Gates that the
+ *                       fused tile engine does not take (a U2 whose control overlaps its b bit) are
+ *                       rejected with QVNT_ERR_UNSUPPORTED.
+ *   qvnt_batch_run      replays the graph: states reset to their basis states, every circuit applied,
+ *                       every measurement taken with its injected draw u01[i] in [0, 1) (required when
+ *                       any mask is non-zero); measured[i] = the CReg value (0 where the mask is 0).
+ *   qvnt_batch_set_fusion / qvnt_batch_autotune
+ *                       re-plan with a tile width (fusion_k, 6..12) and pass budget (estimated FP32
+ *                       instructions per amplitude a pass may hold; 0 = the engine default), or pick
+ *                       both by timing the schedule of every stride-th register under each candidate.
+ *   qvnt_batch_get_amplitudes  register `index` after the last run, interleaved (re, im) f64.
+ *   qvnt_batch_info     schedule items and passes, state bytes, fusion width, pass budget, and the
+ *                       device time of the last run (events around the graph launch).
+ * ------------------------------------------------------------------------------------------- */
+/* Seeded synthetic layers for the batch and serving workloads (no counterpart in the reference):
+ * per layer one gate from {h, s, t, u3} on every qubit, 15 gates from {rxx, ryy, rzz, swap, i_swap,
+ * sqrt_i_swap} on random distinct pairs and 3 Toffolis, drawn from the SplitMix64 state
+ * *rng_state, which is advanced in place (also when cap is too small: gates are then only counted).
+ * Same draws, same gates as the Python generator qvnt_gb300.circuits.random_layers. */
+int qvnt_workload_random_layers(uint32_t n, uint32_t depth, uint64_t* rng_state, qvnt_gate* out, size_t cap,
+                                size_t* count);
+
+typedef struct qvnt_batch qvnt_batch;
+int qvnt_batch_create(qvnt_ctx* ctx, uint32_t count, const uint32_t* q_nums, const uint64_t* states,
+                      const qvnt_gate* gates, const uint64_t* gate_offsets, const uint64_t* measure_masks,
+                      qvnt_batch** out);
+int qvnt_batch_destroy(qvnt_batch* batch);
+int qvnt_batch_run(qvnt_batch* batch, const double* u01, uint64_t* measured);
+int qvnt_batch_set_fusion(qvnt_batch* batch, uint32_t fusion_k, uint32_t pass_budget);
+int qvnt_batch_autotune(qvnt_batch* batch, uint32_t stride, uint32_t* fusion_k, uint32_t* pass_budget,
+                        double* best_ms);
+int qvnt_batch_get_amplitudes(qvnt_batch* batch, uint32_t index, double* out);
+int qvnt_batch_info(const qvnt_batch* batch, uint64_t* items, uint64_t* passes, uint64_t* state_bytes,
+                    uint32_t* fusion_k, uint32_t* pass_budget, double* last_ms);
+
+/* ---------------------------------------------------------------------------------------------
+ * Serving form: a request loop with continuous admission.  A request is one register's life:
+ * `QReg::with_state(q_num, state)` (src/register/quant.rs:113-150), then its calls in order on the
+ * resident state -- QVNT_CALL_APPLY applies the next `gate_count` gates of the request's gate list
+ * (`QReg::apply`, quant.rs:376-395), QVNT_CALL_MEASURE is `measure_mask(mask)` with the injected draw
+ * u01 (quant.rs:490-501).  No counterpart in the reference, whose QReg is driven by one caller.
+ *
+ *   qvnt_server_create   `slots` worker threads; requests are admitted while the states of the
+ *                        running ones fit `hbm_budget_bytes` (16 B per amplitude, plus the same again
+ *                        for a request that keeps its amplitudes); the first queued request that fits
+ *                        goes next, except that a head request older than 0.5 s blocks bypassing.
+ *                        Requests beyond `max_queue` queued ones are shed (QVNT_ERR_BUSY; 0 = 4096).
+ *   qvnt_server_submit   copies the request (gates validated against the register); `arrival_s` is
+ *                        its arrival on the server clock (qvnt_server_clock; < 0 = now), the start of
+ *                        its latency.  flags: QVNT_SUBMIT_KEEP_AMPLITUDES keeps the final state for
+ *                        qvnt_server_wait; QVNT_SUBMIT_DETACHED releases the request when it completes
+ *                        (no wait; its latency still enters the statistics).
+ *   qvnt_server_wait     blocks (timeout_s < 0: without limit) until the request completes; results
+ *                        gets one value per call (the measured value; 0 for APPLY), amplitudes the
+ *                        final state (interleaved f64, max(2^q_num, 8) amplitudes) when kept.
+ *   qvnt_server_latencies / qvnt_server_queued_ages
+ *                        completion latencies (seconds, in completion order) and the waiting times
+ *                        of the requests still queued.
+ *   qvnt_server_destroy  finishes the running requests, fails the queued ones; no wait may be in
+ *                        progress on another thread.
+ * ------------------------------------------------------------------------------------------- */
+#define QVNT_CALL_APPLY 0u
+#define QVNT_CALL_MEASURE 1u
+#define QVNT_SUBMIT_KEEP_AMPLITUDES 1
+#define QVNT_SUBMIT_DETACHED 2
+
+typedef struct qvnt_call {
+    uint32_t op;          /* QVNT_CALL_APPLY or QVNT_CALL_MEASURE */
+    uint32_t reserved;
+    uint64_t gate_count;  /* APPLY: gates taken from the request's list */
+    uint64_t mask;        /* MEASURE: mask */
+    double u01;           /* MEASURE: uniform draw in [0, 1) */
+} qvnt_call;
+
+typedef struct qvnt_server_counters {
+    uint64_t submitted, shed, completed, failed, queued, running, peak_running;
+    uint64_t bytes_active, bytes_pooled;
+    double now_s;
+} qvnt_server_counters;
+
+typedef struct qvnt_server qvnt_server;
+int qvnt_server_create(qvnt_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t slots, uint32_t max_queue,
+                       qvnt_server** out);
+int qvnt_server_destroy(qvnt_server* server);
+int qvnt_server_clock(qvnt_server* server, double* now_s);
+int qvnt_server_submit(qvnt_server* server, uint32_t q_num, uint64_t state, const qvnt_gate* gates,
+                       const qvnt_call* calls, uint32_t ncalls, double arrival_s, int flags, uint64_t* id);
+int qvnt_server_wait(qvnt_server* server, uint64_t id, double timeout_s, uint64_t* results, double* amplitudes,
+                     double* latency_s);
+int qvnt_server_stats(qvnt_server* server, qvnt_server_counters* out);
+int qvnt_server_latencies(qvnt_server* server, double* out, size_t cap, size_t* count);
+int qvnt_server_queued_ages(qvnt_server* server, double* out, size_t cap, size_t* count);
 
 #ifdef __cplusplus
 }

@@ -10,7 +10,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libqvnt_gb300.so")
 
 # enum qvnt_status
-OK, ERR_OOM, ERR_BAD_MASK, ERR_BAD_HANDLE, ERR_CUDA, ERR_TIMEOUT, ERR_BAD_ARG, ERR_UNSUPPORTED = range(8)
+OK, ERR_OOM, ERR_BAD_MASK, ERR_BAD_HANDLE, ERR_CUDA, ERR_TIMEOUT, ERR_BAD_ARG, ERR_UNSUPPORTED, ERR_BUSY = range(9)
 
 # enum qvnt_gate_kind (order of qvnt's AtomicOpDispatch, src/operator/atomic/dispatch.rs:82-105)
 KINDS = ["ID", "X", "RX", "RXX", "Y", "RY", "RYY", "Z", "S", "T", "RZ", "RZZ", "U1", "U2", "H1", "H2",
@@ -36,6 +36,27 @@ class QvntGate(ctypes.Structure):
 
 
 assert ctypes.sizeof(QvntGate) == 304
+
+CALL_APPLY, CALL_MEASURE = 0, 1
+SUBMIT_KEEP_AMPLITUDES, SUBMIT_DETACHED = 1, 2
+
+
+class QvntCall(ctypes.Structure):
+    """`qvnt_call`: one call of a served request (apply the next gate_count gates, or measure)."""
+
+    _fields_ = [
+        ("op", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("gate_count", ctypes.c_uint64),
+        ("mask", ctypes.c_uint64),
+        ("u01", ctypes.c_double),
+    ]
+
+
+class ServerCounters(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint64) for name in ("submitted", "shed", "completed", "failed", "queued",
+                                                      "running", "peak_running", "bytes_active", "bytes_pooled")] + [
+        ("now_s", ctypes.c_double)]
 
 
 class QvntError(RuntimeError):
@@ -100,6 +121,22 @@ _PROTOS = {
     "qvnt_norm_sqr_noalloc": (c_int, [c_void, c_u64, c_void, c_void]),
     "qvnt_reg_stats": (c_int, [c_void, P(c_u64), P(c_u64)]),
     "qvnt_reg_kernel_timing": (c_int, [c_void, c_int, P(c_double), P(c_u64)]),
+    "qvnt_workload_random_layers": (c_int, [c_u32, c_u32, P(c_u64), P(QvntGate), c_size, P(c_size)]),
+    "qvnt_batch_create": (c_int, [c_void, c_u32, P(c_u32), P(c_u64), P(QvntGate), P(c_u64), P(c_u64), P(c_void)]),
+    "qvnt_batch_destroy": (c_int, [c_void]),
+    "qvnt_batch_run": (c_int, [c_void, P(c_double), P(c_u64)]),
+    "qvnt_batch_set_fusion": (c_int, [c_void, c_u32, c_u32]),
+    "qvnt_batch_autotune": (c_int, [c_void, c_u32, P(c_u32), P(c_u32), P(c_double)]),
+    "qvnt_batch_get_amplitudes": (c_int, [c_void, c_u32, c_void]),
+    "qvnt_batch_info": (c_int, [c_void, P(c_u64), P(c_u64), P(c_u64), P(c_u32), P(c_u32), P(c_double)]),
+    "qvnt_server_create": (c_int, [c_void, c_u64, c_u32, c_u32, P(c_void)]),
+    "qvnt_server_destroy": (c_int, [c_void]),
+    "qvnt_server_clock": (c_int, [c_void, P(c_double)]),
+    "qvnt_server_submit": (c_int, [c_void, c_u32, c_u64, P(QvntGate), P(QvntCall), c_u32, c_double, c_int, P(c_u64)]),
+    "qvnt_server_wait": (c_int, [c_void, c_u64, c_double, P(c_u64), c_void, P(c_double)]),
+    "qvnt_server_stats": (c_int, [c_void, P(ServerCounters)]),
+    "qvnt_server_latencies": (c_int, [c_void, P(c_double), c_size, P(c_size)]),
+    "qvnt_server_queued_ages": (c_int, [c_void, P(c_double), c_size, P(c_size)]),
 }
 
 

@@ -27,6 +27,7 @@ UNITS = [
     ("fused.cu", []),
     ("gates_plain.cu", ["--fmad=false"]),
     ("measure.cu", ["--fmad=false"]),
+    ("serve.cu", []),
     ("builders.cpp", None),
 ]
 

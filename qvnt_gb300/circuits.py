@@ -11,10 +11,17 @@ that the GPU run, the CPU oracle and the CPU baseline see the same gate list.
                                    qubit, 15 two-qubit gates from {rxx, ryy, rzz, swap, i_swap,
                                    sqrt_i_swap} on random distinct pairs, 3 Toffolis
                                    x(t).c(c1 | c2); then op::qft(all).  (~2,985 gates at n = 30.)
+  batch_workload(count=4096)       registers with n uniform in [8, 20], with_state(n, random basis
+                                   index), each its own random layers with depth uniform in
+                                   [10, 60], then measure_mask(all).
 """
+import ctypes
 import math
 
+import numpy as np
+
 from . import operator as op
+from ._abi import QvntGate, check, lib
 from .operator import MultiOp
 
 _MASK64 = (1 << 64) - 1
@@ -98,6 +105,82 @@ def random_circuit(n=30, depth=40, seed=2, with_qft=True):
     if with_qft:
         ops.append(op.qft((1 << n) - 1))
     return _concat(ops)
+
+
+def random_layers_gates(n, depth, rng):
+    """`random_layers(n, depth, rng)` drawn by the library's C twin of the generator
+    (qvnt_workload_random_layers: same draws, same gates), as a ctypes QvntGate array; advances
+    `rng` exactly as random_layers does."""
+    arr, count = _c_layers(n, depth, rng)
+    return arr, count
+
+
+def _c_layers(n, depth, rng, into=None, at=0):
+    st = ctypes.c_uint64(rng.state)
+    cnt = ctypes.c_size_t()
+    check(lib().qvnt_workload_random_layers(n, depth, ctypes.byref(st), None, 0, ctypes.byref(cnt)))
+    count = cnt.value
+    st = ctypes.c_uint64(rng.state)
+    if into is None:
+        into = (QvntGate * max(count, 1))()
+        at = 0
+    dst = ctypes.cast(ctypes.byref(into, at * ctypes.sizeof(QvntGate)), ctypes.POINTER(QvntGate))
+    check(lib().qvnt_workload_random_layers(n, depth, ctypes.byref(st), dst, count, ctypes.byref(cnt)))
+    rng.state = st.value
+    return into, count
+
+
+class BatchWorkload:
+    """Registers for the batching form: q_nums, initial basis states, concatenated gate lists with
+    offsets, measure masks."""
+
+    def __init__(self, q_nums, states, depths, gates, offsets, masks):
+        self.q_nums, self.states, self.depths = q_nums, states, depths
+        self.gates, self.offsets, self.masks = gates, offsets, masks
+
+    @property
+    def count(self):
+        return len(self.q_nums)
+
+    @property
+    def total_gates(self):
+        return int(self.offsets[-1])
+
+    def gates_of(self, i):
+        """(ctypes pointer, count) of register i's gate list."""
+        a, b = int(self.offsets[i]), int(self.offsets[i + 1])
+        return ctypes.cast(ctypes.byref(self.gates, a * ctypes.sizeof(QvntGate)), ctypes.POINTER(QvntGate)), b - a
+
+
+def batch_workload(count=4096, seed=4, q_range=(8, 20), depth_range=(10, 60), measure=True):
+    """The batching workload: `count` registers, qubit counts uniform in q_range, each
+    `with_state(n, uniform basis index)` and its own circuit of random layers (the gate mix of
+    random_circuit) with depth uniform in depth_range, then measure_mask of all qubits."""
+    rng = SplitMix64(seed)
+    q_nums = np.zeros(count, dtype=np.uint32)
+    states = np.zeros(count, dtype=np.uint64)
+    depths = np.zeros(count, dtype=np.uint32)
+    seeds = np.zeros(count, dtype=np.uint64)
+    for i in range(count):
+        n = q_range[0] + rng.below(q_range[1] - q_range[0] + 1)
+        q_nums[i] = n
+        states[i] = rng.below(1 << n)
+        depths[i] = depth_range[0] + rng.below(depth_range[1] - depth_range[0] + 1)
+        seeds[i] = rng.next_u64()
+    counts = np.zeros(count, dtype=np.uint64)
+    for i in range(count):
+        st = ctypes.c_uint64(int(seeds[i]))
+        cnt = ctypes.c_size_t()
+        check(lib().qvnt_workload_random_layers(int(q_nums[i]), int(depths[i]), ctypes.byref(st), None, 0,
+                                                ctypes.byref(cnt)))
+        counts[i] = cnt.value
+    offsets = np.zeros(count + 1, dtype=np.uint64)
+    offsets[1:] = np.cumsum(counts)
+    gates = (QvntGate * max(int(offsets[-1]), 1))()
+    for i in range(count):
+        _c_layers(int(q_nums[i]), int(depths[i]), SplitMix64(int(seeds[i])), gates, int(offsets[i]))
+    masks = np.array([(1 << int(n)) - 1 if measure else 0 for n in q_nums], dtype=np.uint64)
+    return BatchWorkload(q_nums, states, depths, gates, offsets, masks)
 
 
 def inverse(circuit):

@@ -246,6 +246,27 @@ constexpr uint32_t kMaxQubits = 40;
 inline bool ctx_ok(const qvnt_ctx* c) { return c && c->magic == kMagicCtx; }
 inline bool reg_ok(const qvnt_reg* r) { return r && r->magic == kMagicReg; }
 
+}  // namespace
+
+bool qvnt::ctx_valid(const qvnt_ctx* c) { return ctx_ok(c); }
+
+int qvnt::reg_set_priority(qvnt_reg* r, int priority) {
+    if (!reg_ok(r)) return set_error(QVNT_ERR_BAD_HANDLE, "invalid register handle");
+    QVNT_CUDA_TRY(cudaSetDevice(r->ctx->device));
+    cudaStream_t s = nullptr;
+    QVNT_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, priority));
+    cudaError_t e = cudaStreamSynchronize(r->stream);
+    if (e == cudaSuccess) e = cudaStreamDestroy(r->stream);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return set_cuda_error(e, "stream replacement");
+    }
+    r->stream = s;
+    return QVNT_OK;
+}
+
+namespace {
+
 #define CHECK_REG(r) \
     if (!reg_ok(r)) return set_error(QVNT_ERR_BAD_HANDLE, "invalid register handle")
 #define CHECK_CTX(c) \
@@ -293,6 +314,7 @@ const char* qvnt_status_string(int status) {
     case QVNT_ERR_TIMEOUT: return "device wait timed out";
     case QVNT_ERR_BAD_ARG: return "invalid argument";
     case QVNT_ERR_UNSUPPORTED: return "unsupported";
+    case QVNT_ERR_BUSY: return "queue full";
     default: return "unknown status";
     }
 }

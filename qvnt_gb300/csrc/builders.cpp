@@ -380,6 +380,76 @@ int qvnt_ops_dgr(qvnt_gate* gates, size_t count) {  // multi/mod.rs:120-123
     return QVNT_OK;
 }
 
+// Seeded synthetic layers (the generator of qvnt_gb300/circuits.py `random_layers`, here for the
+// batch and serving workloads that need thousands of circuits): per layer one gate from
+// {h, s, t, u3(th, phi, lam)} on every qubit, 15 two-qubit gates from {rxx, ryy, rzz, swap, i_swap,
+// sqrt_i_swap} on random distinct pairs, 3 Toffolis x(t).c(c1 | c2).  The SplitMix64 state is
+// advanced in place, also when `out` is too small (the gates are then counted, not written).
+int qvnt_workload_random_layers(uint32_t n, uint32_t depth, uint64_t* rng_state, qvnt_gate* out, size_t cap,
+                                size_t* count) {
+    if (!rng_state) return set_error(QVNT_ERR_BAD_ARG, "null rng state");
+    if (n < 3 || n > 63) return set_error(QVNT_ERR_BAD_ARG, "n = %u: the layer generator needs 3..63 qubits", n);
+    uint64_t& st = *rng_state;
+    auto next = [&]() {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    auto uniform = [&]() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); };
+    auto below = [&](uint64_t m) { return next() % m; };
+    const double two_pi = 2.0 * M_PI;
+    GateList gl{out, cap};
+    qvnt_gate g;
+    for (uint32_t layer = 0; layer < depth; ++layer) {
+        for (uint32_t q = 0; q < n; ++q) {
+            const uint64_t m = 1ull << q;
+            switch (below(4)) {
+            case 0: build_h(m, gl); break;
+            case 1: make(QVNT_GATE_S, m, 0, 0, nullptr, &g); gl.push(g); break;
+            case 2: make(QVNT_GATE_T, m, 0, 0, nullptr, &g); gl.push(g); break;
+            default: {
+                const double th = two_pi * uniform(), ph = two_pi * uniform(), la = two_pi * uniform();
+                make(QVNT_GATE_RZ, m, 0, la, nullptr, &g);  // u3 = rz(la) ry(th) rz(ph), mod.rs:499-501
+                gl.push(g);
+                make(QVNT_GATE_RY, m, 0, th, nullptr, &g);
+                gl.push(g);
+                make(QVNT_GATE_RZ, m, 0, ph, nullptr, &g);
+                gl.push(g);
+            }
+            }
+        }
+        for (int i = 0; i < 15; ++i) {
+            const uint64_t a = below(n);
+            uint64_t b = below(n - 1);
+            if (b >= a) ++b;
+            const uint64_t ab = (1ull << a) | (1ull << b);
+            const uint64_t kind = below(6);
+            if (kind < 3) {
+                const uint32_t kinds[3] = {QVNT_GATE_RXX, QVNT_GATE_RYY, QVNT_GATE_RZZ};
+                make(kinds[kind], ab, 0, two_pi * uniform(), nullptr, &g);
+            } else {
+                const uint32_t kinds[3] = {QVNT_GATE_SWAP, QVNT_GATE_ISWAP, QVNT_GATE_SQRT_ISWAP};
+                make(kinds[kind - 3], ab, 0, 0, nullptr, &g);
+            }
+            gl.push(g);
+        }
+        for (int i = 0; i < 3; ++i) {
+            const uint64_t t = below(n);
+            uint64_t c1 = below(n - 1);
+            if (c1 >= t) ++c1;
+            uint64_t c2 = below(n);
+            while (c2 == t || c2 == c1) c2 = below(n);
+            make(QVNT_GATE_X, 1ull << t, 0, 0, nullptr, &g);
+            g.ctrl = (1ull << c1) | (1ull << c2);
+            gl.push(g);
+        }
+    }
+    if (count) *count = gl.n;
+    return QVNT_OK;
+}
+
 int qvnt_ops_c(qvnt_gate* gates, size_t count, uint64_t c_mask) {  // multi/mod.rs:125-132
     if (!gates && count) return set_error(QVNT_ERR_BAD_ARG, "null gate list");
     uint64_t act = 0;

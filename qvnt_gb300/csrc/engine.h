@@ -59,6 +59,8 @@ struct qvnt_reg {
 };
 
 namespace qvnt {
+bool ctx_valid(const qvnt_ctx* c);
+int reg_set_priority(qvnt_reg* r, int priority);  // replaces the register's stream by one of this priority
 int validate_gate(const qvnt_gate& g, uint64_t len);
 uint64_t gate_acts_on(const qvnt_gate& g);
 int gate_check_masks(const qvnt_gate& g);
