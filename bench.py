@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1, help="steps of the plain f64 GPU path (0 = skip)")
+    ap.add_argument("--forms", default="batch,serve", help="extra forms to measure: batch, serve (empty = none)")
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     return ap.parse_args()
 
 
@@ -172,6 +176,97 @@ def cpu_sample(circ_gates, n, budget_s=12.0):
         t_total += time.perf_counter() - t0
         done += 1
     return done / t_total, threads, done
+
+
+def bench_batch(ctx, count, steps):
+    """Batching form: `count` registers (n uniform in [8, 20], depth uniform in [10, 60], random basis
+    state, measure_mask of all qubits) in one persistent launch per run, tile width and pass budget
+    autotuned on every 16th register.  Beside it, the plain f64 GPU path (one register at a time,
+    one pass per gate) on every 64th register, extrapolated to the batch."""
+    import numpy as np
+    from qvnt_gb300 import ENGINE_PLAIN, QReg
+    from qvnt_gb300.batch import Batch
+    from qvnt_gb300.circuits import SplitMix64, batch_workload
+
+    w = batch_workload(count=count)
+    b = Batch(w.q_nums, w.states, w.gates, w.offsets, w.masks, ctx=ctx)
+    k, budget, tune_ms = b.autotune(stride=16)
+    rng = SplitMix64(17)
+    u01 = np.array([rng.uniform() for _ in range(w.count)])
+    b.run(u01)  # warm-up
+    ms = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        b.run(u01)
+        ms.append(b.info()["last_ms"])
+    wall = time.perf_counter() - t0
+    info = b.info()
+    b.close()
+    dev_s = sum(ms) / 1e3
+    sample = list(range(0, w.count, 64))
+    import torch
+    t_plain = 0.0
+    for i in sample:
+        q = QReg.with_state(int(w.q_nums[i]), int(w.states[i]), ctx=ctx)
+        q.set_engine(ENGINE_PLAIN)
+        ptr, cnt = w.gates_of(i)
+        q.sync()
+        t1 = time.perf_counter()
+        q.apply_gates(ptr, cnt)
+        q.measure_mask(int(w.masks[i]), u01=float(u01[i]))
+        q.sync()
+        t_plain += time.perf_counter() - t1
+        q.close()
+    torch.cuda.synchronize()
+    plain_cps = len(sample) / t_plain
+    return {"workload": "%d registers, n uniform [8, 20], depth uniform [10, 60] random layers, measure_mask(all)"
+                        % w.count,
+            "circuits_per_s": w.count * steps / dev_s, "gate_passes_per_s": w.total_gates * steps / dev_s,
+            "ms_per_run": dev_s * 1e3 / steps, "e2e_circuits_per_s": w.count * steps / wall,
+            "gates": w.total_gates, "state_bytes": info["state_bytes"], "schedule_items": info["items"],
+            "passes": info["passes"], "fusion_k": k, "pass_budget": budget, "autotune_best_sample_ms": tune_ms,
+            "launches_per_run": 1, "dtype": "double-float (f64-equivalent), 1e-12 parity",
+            "plain_f64_gpu": {"circuits_per_s": plain_cps, "sample": "every 64th register (%d), one at a time"
+                              % len(sample)}}
+
+
+def bench_serve(ctx, rate, seconds):
+    """Serving form: Poisson arrivals at `rate`/s for `seconds` s (n log-uniform [10, 28], depth
+    uniform [5, 100] over 1-3 apply/measure rounds, 150 GB HBM budget, 16 slots, queue of 1024);
+    then 5 s to drain.  Latency = completion - scheduled arrival."""
+    import numpy as np
+    from qvnt_gb300.circuits import serve_requests
+    from qvnt_gb300.serve import Server
+
+    max_queue = 1024
+    s = Server(budget_bytes=150 * 10**9, slots=16, max_queue=max_queue, ctx=ctx)
+    t0 = s.clock()
+    offered = shed = 0
+    for r in serve_requests(rate=rate, duration=seconds, seed=5):
+        offered += 1
+        lag = r.arrival - (s.clock() - t0)
+        if lag > 0:
+            time.sleep(lag)
+        if s.stats()["queued"] >= max_queue:
+            shed += 1  # shed without building the circuit
+            continue
+        gates, calls = r.build()
+        if s.submit(r.n, r.state, gates, calls, arrival=t0 + r.arrival, detached=True) is None:
+            shed += 1
+    time.sleep(5.0)
+    st = s.stats()
+    lat = s.latencies()
+    ages = s.queued_ages()
+    elapsed = s.clock() - t0
+    s.close()
+    pct = (lambda a, p: float(np.percentile(a, p)) * 1e3 if a.size else None)
+    censored = np.concatenate([lat, ages]) if ages.size else lat
+    return {"workload": "Poisson %.0f req/s for %.0f s, n log-uniform [10, 28], depth uniform [5, 100], "
+                        "1-3 apply/measure rounds, 150 GB budget, 16 slots" % (rate, seconds),
+            "offered": offered, "submitted": st["submitted"], "shed": shed, "completed": st["completed"],
+            "failed": st["failed"], "queued_at_end": st["queued"], "running_at_end": st["running"],
+            "served_circuits_per_s": st["completed"] / elapsed, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
+            "p99_ms_incl_queued": pct(censored, 99), "peak_running": st["peak_running"], "elapsed_s": elapsed}
 
 
 def run_reference(args, ws, rank):
@@ -334,6 +429,21 @@ def main():
                "h2d_bytes_per_step": length * AMP_BYTES + ngates * ctypes.sizeof(gates[0]),
                "d2h_bytes_per_step": length * AMP_BYTES}
 
+    forms = {}
+    if args.no_e2e:  # the e2e leg has already released the 30-qubit register
+        q.close()
+        del q
+    if rank == 0:
+        torch.cuda.synchronize()
+        for form in [f for f in args.forms.split(",") if f]:
+            try:
+                if form == "batch":
+                    forms["batch"] = bench_batch(ctx, args.batch_count, max(1, args.steps))
+                elif form == "serve":
+                    forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds)
+            except Exception as exc:  # a form's failure is reported, not hidden
+                forms[form] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, threads, done = cpu_sample(gates, n)
@@ -371,6 +481,7 @@ def main():
             "e2e": e2e,
             "gpu_launches": gpu_launches,
             "clocks": clk,
+            "forms": forms,
         }
         print(json.dumps(line), flush=True)
     dist.close()

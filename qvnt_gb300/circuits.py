@@ -183,6 +183,67 @@ def batch_workload(count=4096, seed=4, q_range=(8, 20), depth_range=(10, 60), me
     return BatchWorkload(q_nums, states, depths, gates, offsets, masks)
 
 
+class ServeRequest:
+    """One served request: arrival time (s), register size and basis state, and its calls: rounds
+    of (apply `depths[i]` random layers, measure_mask(masks[i]) with draw u01s[i])."""
+
+    __slots__ = ("arrival", "n", "state", "depths", "masks", "u01s", "seed")
+
+    def __init__(self, arrival, n, state, depths, masks, u01s, seed):
+        self.arrival, self.n, self.state = arrival, n, state
+        self.depths, self.masks, self.u01s, self.seed = depths, masks, u01s, seed
+
+    def build(self):
+        """(gate array, calls) for Server.submit."""
+        rng = SplitMix64(self.seed)
+        counts = []
+        for d in self.depths:
+            st = ctypes.c_uint64(rng.state)
+            cnt = ctypes.c_size_t()
+            check(lib().qvnt_workload_random_layers(self.n, d, ctypes.byref(st), None, 0, ctypes.byref(cnt)))
+            counts.append(cnt.value)
+            rng.state = st.value
+        gates = (QvntGate * max(sum(counts), 1))()
+        rng = SplitMix64(self.seed)
+        at = 0
+        calls = []
+        for d, c, m, u in zip(self.depths, counts, self.masks, self.u01s):
+            _c_layers(self.n, d, rng, gates, at)
+            at += c
+            calls.append(("apply", c))
+            calls.append(("measure", m, u))
+        return gates, calls
+
+
+def serve_requests(rate=2000.0, duration=60.0, seed=5, q_range=(10, 28), depth_range=(5, 100)):
+    """The serving workload: Poisson arrivals at `rate` per second over `duration` seconds; qubit
+    count log-uniform in q_range, depth uniform in depth_range split over 1-3 rounds of apply then
+    measure_mask (of 1-3 random qubits).  Yields ServeRequest in arrival order."""
+    rng = SplitMix64(seed)
+    t = 0.0
+    lo, hi = math.log(q_range[0]), math.log(q_range[1] + 1)
+    while True:
+        t += -math.log(1.0 - rng.uniform()) / rate
+        if t >= duration:
+            return
+        n = min(q_range[1], int(math.exp(lo + (hi - lo) * rng.uniform())))
+        state = rng.below(1 << n)
+        depth = depth_range[0] + rng.below(depth_range[1] - depth_range[0] + 1)
+        rounds = min(depth, 1 + rng.below(3))
+        cuts = sorted(rng.below(depth - 1) + 1 for _ in range(rounds - 1)) if rounds > 1 else []
+        bounds = [0] + cuts + [depth]
+        depths = [bounds[i + 1] - bounds[i] for i in range(rounds)]
+        depths = [d for d in depths if d > 0] or [depth]
+        masks, u01s = [], []
+        for _ in depths:
+            m = 0
+            for _ in range(1 + rng.below(3)):
+                m |= 1 << rng.below(n)
+            masks.append(m)
+            u01s.append(rng.uniform())
+        yield ServeRequest(t, n, state, depths, masks, u01s, rng.next_u64())
+
+
 def inverse(circuit):
     """The true inverse of a circuit.  qvnt's `.dgr()` maps a rotation R(theta) to -R(theta)
     (its stored phase is negated, src/operator/atomic/rx.rs:42-47), so it is not an inverse for

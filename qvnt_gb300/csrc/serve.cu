@@ -6,15 +6,16 @@
 // that stays resident in HBM between the calls.
 //
 // `slots` worker threads each run one request at a time on the request's own CUDA stream, so the
-// kernels of different requests overlap on the device.  A worker that frees up admits the first
-// queued request whose state fits the HBM budget next to the running ones (FIFO with backfill; a
-// head request that has waited longer than `kHolLimit` stops the backfill until it is admitted).
+// kernels of different requests overlap on the device.  A worker that frees up admits, among the
+// queued requests whose state fits the HBM budget next to the running ones, the one with the least
+// estimated work discounted by its waiting time (shortest first, with ageing).
 // Registers are pooled by size and reused through `qvnt_reg_reset`, so steady-state admission
 // allocates nothing and never hits the device-wide synchronisation of cudaFree; idle pooled
 // registers are freed only when a new size needs their memory.  Streams of small registers get the
 // higher stream priority, so their blocks overtake the long passes of large ones.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -32,7 +33,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr uint32_t kMagicServer = 0x51535256u;
-constexpr double kHolLimit = 0.5;  // seconds a head request may be bypassed by smaller ones
+constexpr double kAgeScale = 1.0;  // seconds: waiting time that discounts a request's work by e
 
 struct Request {
     uint64_t id = 0;
@@ -44,6 +45,7 @@ struct Request {
     bool keep_amplitudes = false;
     bool detached = false;
     uint64_t footprint = 0;
+    double work = 0.0;  // amplitudes x gates (+ amplitudes per measurement)
     // results
     int status = QVNT_OK;
     std::string error;
@@ -95,16 +97,24 @@ int priority_for(const qvnt_server* s, uint32_t n) {
     return s->prio_least;
 }
 
-// Picks the request to admit (caller holds the lock): the first that fits, the head only once it
-// has waited past the bypass limit.  Returns queue.end() when none fits.
+// Picks the request to admit (caller holds the lock): among the queued requests whose state fits
+// next to the running ones, the least estimated work (amplitudes x gates) discounted by waiting time,
+// work * exp(-age / kAgeScale): short requests go first, and a long one overtakes a fresh short one
+// after waiting about kAgeScale * ln(work ratio).  Returns queue.end() when none fits.
 std::deque<Request*>::iterator pick(qvnt_server* s) {
     const double t = s->now();
+    auto best = s->queue.end();
+    double best_score = 0.0;
     for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
         // idle pooled registers are reused or evicted, so only running requests hold memory
-        if (s->bytes_active + (*it)->footprint <= s->budget) return it;
-        if (it == s->queue.begin() && t - (*it)->arrival > kHolLimit) break;
+        if (s->bytes_active + (*it)->footprint > s->budget) continue;
+        const double score = (*it)->work * std::exp(-(t - (*it)->arrival) / kAgeScale);
+        if (best == s->queue.end() || score < best_score) {
+            best = it;
+            best_score = score;
+        }
     }
-    return s->queue.end();
+    return best;
 }
 
 int run_request(qvnt_server* s, Request* r, qvnt_reg* reg) {
@@ -275,6 +285,7 @@ extern "C" int qvnt_server_submit(qvnt_server* s, uint32_t q_num, uint64_t state
     r->keep_amplitudes = (flags & QVNT_SUBMIT_KEEP_AMPLITUDES) != 0;
     r->detached = (flags & QVNT_SUBMIT_DETACHED) != 0;
     r->footprint = fp;
+    r->work = (double)len * (double)(ng + ncalls);
     std::lock_guard<std::mutex> lk(s->mu);
     r->arrival = arrival_s >= 0.0 ? arrival_s : s->now();
     if (s->queue.size() >= s->max_queue) {
