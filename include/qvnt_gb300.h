@@ -102,8 +102,12 @@ typedef struct qvnt_reg qvnt_reg;
 /* Engines a register can run its gate queue on.
  *   FUSED  (default) groups runs of gates into fused passes staged through shared memory.
  *   PLAIN  runs one in-place FP64 pass per `SingleOp`, in qvnt's own operand order; its amplitudes
- *          are bit-identical to qvnt's non-fast-math arithmetic.  It is the plain f64 GPU path. */
-enum qvnt_engine { QVNT_ENGINE_FUSED = 0, QVNT_ENGINE_PLAIN = 1 };
+ *          are bit-identical to qvnt's non-fast-math arithmetic.  It is the plain f64 GPU path.
+ *   PRECISION keeps complex<f32> amplitudes (8 B) and fuses runs of gates into dense 5-qubit blocks
+ *          (32 x 32 complex) contracted on the tensor cores (TF32 split hi + lo, FP32 accumulation);
+ *          norms, probabilities and measurement stay FP64.  Registers of at least 12 qubits; gates
+ *          whose targets and controls span more than 5 qubits are rejected (QVNT_ERR_UNSUPPORTED). */
+enum qvnt_engine { QVNT_ENGINE_FUSED = 0, QVNT_ENGINE_PLAIN = 1, QVNT_ENGINE_PRECISION = 2 };
 
 /* ---------------------------------------------------------------------------------------------
  * Status / errors
@@ -128,6 +132,9 @@ int qvnt_ctx_mem_info(qvnt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes
 /* `QReg::with_state(q_num, state)`; `QReg::new(q_num)` is state = 0.  The state index is masked
  * by 2^q_num - 1 as in quant.rs:131-142.  q_num <= 40. */
 int qvnt_reg_create(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, qvnt_reg** out);
+/* As qvnt_reg_create, on a chosen engine (enum qvnt_engine): a PRECISION register is allocated at
+ * 8 B per amplitude from the start. */
+int qvnt_reg_create_ex(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, int engine, qvnt_reg** out);
 int qvnt_reg_destroy(qvnt_reg* reg);
 /* `QReg::clone` (derive(Clone), quant.rs:102). */
 int qvnt_reg_clone(const qvnt_reg* reg, qvnt_reg** out);
@@ -258,6 +265,13 @@ int qvnt_norm_sqr_noalloc(const double* d_psi, uint64_t len, double* d_out, void
  * Counters for measurement: kernels launched and fused passes run by this register so far.
  * ------------------------------------------------------------------------------------------- */
 int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* passes);
+/* State comparison in FP64 across engines (no counterpart in the reference): fidelity
+ * |<a|b>|^2 / (<a|a> <b|b>) and max_i |a_i - b_i|.  Registers of the same size and context. */
+int qvnt_reg_overlap(const qvnt_reg* a, const qvnt_reg* b, double* fidelity, double* max_abs_diff);
+/* Host-side plan of the precision engine for a gate list on q_num (>= 12) qubits: passes and dense
+ * 5-qubit blocks. */
+int qvnt_precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* passes,
+                             uint64_t* blocks);
 /* Time the fused engine spends in its dominant kernel: CUDA events recorded around every launch of
  * the fused-pass kernel on the register's stream since the last reset (enable != 0 turns
  * recording on and clears the totals).  *ms = summed event time, *launches = number of launches. */

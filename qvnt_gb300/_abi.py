@@ -19,6 +19,7 @@ KIND = {name: i for i, name in enumerate(KINDS)}
 
 ENGINE_FUSED = 0
 ENGINE_PLAIN = 1
+ENGINE_PRECISION = 2
 
 
 class QvntGate(ctypes.Structure):
@@ -83,6 +84,9 @@ _PROTOS = {
     "qvnt_ctx_destroy": (c_int, [c_void]),
     "qvnt_ctx_mem_info": (c_int, [c_void, P(c_u64), P(c_u64)]),
     "qvnt_reg_create": (c_int, [c_void, c_u32, c_u64, P(c_void)]),
+    "qvnt_reg_create_ex": (c_int, [c_void, c_u32, c_u64, c_int, P(c_void)]),
+    "qvnt_reg_overlap": (c_int, [c_void, c_void, P(c_double), P(c_double)]),
+    "qvnt_precision_plan_info": (c_int, [P(QvntGate), c_size, c_u32, P(c_u64), P(c_u64)]),
     "qvnt_reg_destroy": (c_int, [c_void]),
     "qvnt_reg_clone": (c_int, [c_void, P(c_void)]),
     "qvnt_reg_num": (c_int, [c_void, P(c_u32)]),

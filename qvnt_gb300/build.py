@@ -28,6 +28,7 @@ UNITS = [
     ("gates_plain.cu", ["--fmad=false"]),
     ("measure.cu", ["--fmad=false"]),
     ("serve.cu", []),
+    ("precision.cu", []),
     ("builders.cpp", None),
 ]
 

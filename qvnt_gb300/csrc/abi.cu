@@ -105,7 +105,7 @@ DevGate decode_gate(const qvnt_gate& g) {
 int reg_alloc(qvnt_reg* r) {
     QVNT_CUDA_TRY(cudaSetDevice(r->ctx->device));
     QVNT_CUDA_TRY(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking));
-    cudaError_t e = cudaMalloc(&r->psi, r->len * sizeof(amp_t));
+    cudaError_t e = cudaMalloc(&r->psi, r->len * fmt_bytes(r->fmt));
     if (e != cudaSuccess) {
         r->psi = nullptr;
         return set_cuda_error(e, "cudaMalloc(state)");
@@ -282,14 +282,18 @@ uint64_t reg_len_for(uint32_t q_num) {
     return q < 8 ? 8 : q;
 }
 
-int make_reg(qvnt_ctx* ctx, uint32_t q_num, qvnt_reg** out) {
+int fmt_of_engine(int engine) {
+    return engine == QVNT_ENGINE_PLAIN ? FMT_F64 : engine == QVNT_ENGINE_PRECISION ? FMT_C32 : FMT_DF64;
+}
+
+int make_reg(qvnt_ctx* ctx, uint32_t q_num, int engine, qvnt_reg** out) {
     qvnt_reg* r = new qvnt_reg();
     r->magic = kMagicReg;
     r->ctx = ctx;
     r->q_num = q_num;
     r->len = reg_len_for(q_num);
-    r->engine = ctx->default_engine;
-    r->fmt = r->engine == QVNT_ENGINE_PLAIN ? FMT_F64 : FMT_DF64;
+    r->engine = engine;
+    r->fmt = fmt_of_engine(engine);
     int st = reg_alloc(r);
     if (st) {
         std::string msg = qvnt_last_error();
@@ -361,10 +365,17 @@ int qvnt_ctx_mem_info(qvnt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes
 
 int qvnt_reg_create(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, qvnt_reg** out) {
     CHECK_CTX(ctx);
+    return qvnt_reg_create_ex(ctx, q_num, state, ctx->default_engine, out);
+}
+
+int qvnt_reg_create_ex(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, int engine, qvnt_reg** out) {
+    CHECK_CTX(ctx);
     if (!out) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
     if (q_num > kMaxQubits) return set_error(QVNT_ERR_BAD_ARG, "q_num %u > %u", q_num, kMaxQubits);
+    if (engine != QVNT_ENGINE_FUSED && engine != QVNT_ENGINE_PLAIN && engine != QVNT_ENGINE_PRECISION)
+        return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
     qvnt_reg* r = nullptr;
-    TRY(make_reg(ctx, q_num, &r));
+    TRY(make_reg(ctx, q_num, engine, &r));
     const uint64_t q_mask = (1ull << q_num) - 1;
     int st = launch_reset(r->psi, r->fmt, r->len, state & q_mask, r->stream);  // quant.rs:129-150
     if (st) {
@@ -385,12 +396,11 @@ int qvnt_reg_clone(const qvnt_reg* reg, qvnt_reg** out) {
     CHECK_REG(reg);
     if (!out) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
     qvnt_reg* r = nullptr;
-    TRY(make_reg(reg->ctx, reg->q_num, &r));
-    r->engine = reg->engine;
-    r->fmt = reg->fmt;
+    TRY(make_reg(reg->ctx, reg->q_num, reg->engine, &r));
     r->fusion_k = reg->fusion_k;
     cudaError_t e = cudaStreamSynchronize(reg->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(r->psi, reg->psi, r->len * sizeof(amp_t), cudaMemcpyDeviceToDevice, r->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(r->psi, reg->psi, r->len * fmt_bytes(r->fmt), cudaMemcpyDeviceToDevice, r->stream);
     if (e != cudaSuccess) {
         reg_free(r);
         return set_cuda_error(e, "clone copy");
@@ -415,10 +425,30 @@ int qvnt_reg_len(const qvnt_reg* reg, uint64_t* len) {
 
 int qvnt_reg_set_engine(qvnt_reg* reg, int engine) {
     CHECK_REG(reg);
-    if (engine != QVNT_ENGINE_FUSED && engine != QVNT_ENGINE_PLAIN)
+    if (engine != QVNT_ENGINE_FUSED && engine != QVNT_ENGINE_PLAIN && engine != QVNT_ENGINE_PRECISION)
         return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
-    TRY(reg_set_format(reg, engine == QVNT_ENGINE_PLAIN ? FMT_F64 : FMT_DF64));
+    const int fmt = fmt_of_engine(engine);
+    if (fmt_bytes(fmt) != fmt_bytes(reg->fmt)) {
+        // element size changes: convert into a new buffer
+        double2* nb = nullptr;
+        cudaError_t e = cudaMalloc(&nb, reg->len * fmt_bytes(fmt));
+        if (e != cudaSuccess) return set_cuda_error(e, "cudaMalloc(state, engine switch)");
+        int st = launch_convert_fmt(reg->psi, reg->fmt, nb, fmt, reg->len, reg->stream);
+        if (st) {
+            cudaFree(nb);
+            return st;
+        }
+        QVNT_CUDA_TRY(cudaStreamSynchronize(reg->stream));
+        cudaFree(reg->psi);
+        if (reg->alt) cudaFree(reg->alt);
+        reg->alt = nullptr;
+        reg->psi = nb;
+        reg->fmt = fmt;
+        reg->launches += 1;
+    } else {
+        TRY(reg_set_format(reg, fmt));
+    }
     reg->engine = engine;
     return QVNT_OK;
 }
@@ -441,6 +471,7 @@ int qvnt_reg_apply(qvnt_reg* reg, const qvnt_gate* gates, size_t count) {
     }
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
     if (reg->engine == QVNT_ENGINE_PLAIN) return apply_plain(reg, gates, count);
+    if (reg->engine == QVNT_ENGINE_PRECISION) return apply_precision(reg, gates, count);
     return apply_fused(reg, gates, count);
 }
 
@@ -577,6 +608,19 @@ int qvnt_reg_set_amplitudes(qvnt_reg* reg, const double* host_in) {
     CHECK_REG(reg);
     if (!host_in) return set_error(QVNT_ERR_BAD_ARG, "null input pointer");
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
+    if (reg->fmt == FMT_C32) {  // through the staging buffer, piecewise
+        const uint64_t piece = reg->len < (1ull << 22) ? reg->len : (1ull << 22);
+        TRY(reg_ensure_staging(reg, piece * sizeof(amp_t)));
+        for (uint64_t at = 0; at < reg->len; at += piece) {
+            const uint64_t n = (reg->len - at) < piece ? (reg->len - at) : piece;
+            QVNT_CUDA_TRY(cudaMemcpyAsync(reg->staging, host_in + 2 * at, n * sizeof(amp_t), cudaMemcpyHostToDevice,
+                                          reg->stream));
+            TRY(launch_copy_in(reg->psi, reg->fmt, at, n, reinterpret_cast<const double2*>(reg->staging), reg->stream));
+            TRY(reg_sync(reg));
+            reg->launches += 1;
+        }
+        return QVNT_OK;
+    }
     QVNT_CUDA_TRY(cudaMemcpyAsync(reg->psi, host_in, reg->len * sizeof(amp_t), cudaMemcpyHostToDevice, reg->stream));
     if (reg->fmt == FMT_DF64) {
         TRY(launch_convert(reg->psi, reg->len, 1, reg->stream));  // f64 -> double-float, in place
@@ -619,15 +663,15 @@ int qvnt_reg_tensor(const qvnt_reg* a, const qvnt_reg* b, qvnt_reg** out) {
     CHECK_REG(b);
     if (!out) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
     if (a->ctx != b->ctx) return set_error(QVNT_ERR_BAD_ARG, "registers belong to different contexts");
+    if (a->fmt == FMT_C32 || b->fmt == FMT_C32)
+        return set_error(QVNT_ERR_UNSUPPORTED, "tensor product of precision-engine registers");
     const uint32_t q_num = a->q_num + b->q_num;
     if (q_num > kMaxQubits) return set_error(QVNT_ERR_BAD_ARG, "tensor product has %u qubits", q_num);
     QVNT_CUDA_TRY(cudaSetDevice(a->ctx->device));
     QVNT_CUDA_TRY(cudaStreamSynchronize(a->stream));
     QVNT_CUDA_TRY(cudaStreamSynchronize(b->stream));
     qvnt_reg* r = nullptr;
-    TRY(make_reg(a->ctx, q_num, &r));
-    r->engine = a->engine;
-    r->fmt = a->fmt;
+    TRY(make_reg(a->ctx, q_num, a->engine, &r));
     int st = launch_tensor(a->psi, a->fmt, a->q_num, b->psi, b->fmt, b->q_num, r->psi, r->fmt, r->len, r->stream);
     if (st) {
         reg_free(r);
@@ -657,7 +701,9 @@ int qvnt_apply_host(qvnt_ctx* ctx, const qvnt_gate* gates, size_t count, const d
         reg_free(ctx->host_reg);
         ctx->host_reg = nullptr;
     }
-    if (!ctx->host_reg) TRY(make_reg(ctx, q_num, &ctx->host_reg));
+    if (!ctx->host_reg)
+        TRY(make_reg(ctx, q_num, ctx->default_engine == QVNT_ENGINE_PLAIN ? QVNT_ENGINE_PLAIN : QVNT_ENGINE_FUSED,
+                     &ctx->host_reg));
     qvnt_reg* r = ctx->host_reg;
     for (size_t k = 0; k < count; ++k) {
         int st = validate_gate(gates[k], r->len);
@@ -680,6 +726,41 @@ int qvnt_reg_get_stream(const qvnt_reg* reg, void** stream) {
     if (!stream) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
     *stream = reinterpret_cast<void*>(reg->stream);
     return QVNT_OK;
+}
+
+int qvnt_reg_overlap(const qvnt_reg* a, const qvnt_reg* b, double* fidelity, double* max_abs_diff) {
+    CHECK_REG(a);
+    CHECK_REG(b);
+    if (a->len != b->len) return set_error(QVNT_ERR_BAD_ARG, "registers of different sizes");
+    if (a->ctx != b->ctx) return set_error(QVNT_ERR_BAD_ARG, "registers belong to different contexts");
+    QVNT_CUDA_TRY(cudaSetDevice(a->ctx->device));
+    QVNT_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    double* d = nullptr;
+    const uint64_t nc = chunk_count(a->len);
+    QVNT_CUDA_TRY(cudaMalloc(&d, (5 * nc + 8) * sizeof(double)));
+    int st = launch_overlap(a->psi, a->fmt, b->psi, b->fmt, a->len, d + 8, d, a->stream);
+    double h[5] = {0, 0, 0, 0, 0};
+    cudaError_t e = st ? cudaSuccess : cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, a->stream);
+    if (e == cudaSuccess && !st) e = cudaStreamSynchronize(a->stream);
+    cudaFree(d);
+    if (st) return st;
+    if (e != cudaSuccess) return set_cuda_error(e, "overlap");
+    // |<a|b>|^2 / (<a|a> <b|b>)
+    if (fidelity) *fidelity = (h[2] > 0 && h[3] > 0) ? (h[0] * h[0] + h[1] * h[1]) / (h[2] * h[3]) : 0.0;
+    if (max_abs_diff) *max_abs_diff = h[4];
+    return QVNT_OK;
+}
+
+int qvnt_precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* passes,
+                             uint64_t* blocks) {
+    if (!gates && count) return set_error(QVNT_ERR_BAD_ARG, "null gate list");
+    if (!passes || !blocks) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
+    if (q_num < 12 || q_num > kMaxQubits) return set_error(QVNT_ERR_BAD_ARG, "q_num %u outside [12, %u]", q_num, kMaxQubits);
+    for (size_t k = 0; k < count; ++k) {
+        int st = validate_gate(gates[k], 1ull << q_num);
+        if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
+    }
+    return precision_plan_info(gates, count, q_num, passes, blocks);
 }
 
 int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* passes) {

@@ -1,5 +1,6 @@
 // The 20 atomic gate functions of qvnt, as device code.
 //
+// Callable from host code too (the precision engine builds dense gate matrices with it).
 // `atomic_op(g, idx, psi)` returns qvnt's `AtomicOp::atomic_op(psi, idx)` for the gate kind, where
 // `psi(j)` yields the input amplitude at index j.  Operand order and association follow each
 // reference file line by line; translation units that include this header are compiled with
@@ -10,16 +11,16 @@
 
 namespace qvnt {
 
-__device__ __forceinline__ amp_t c_add(amp_t a, amp_t b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ amp_t c_neg(amp_t a) { return make_double2(-a.x, -a.y); }
+__host__ __device__ __forceinline__ amp_t c_add(amp_t a, amp_t b) { return make_double2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ amp_t c_neg(amp_t a) { return make_double2(-a.x, -a.y); }
 // num-complex Mul: re = a.re*b.re - a.im*b.im, im = a.re*b.im + a.im*b.re
-__device__ __forceinline__ amp_t c_mul(amp_t a, amp_t b) {
+__host__ __device__ __forceinline__ amp_t c_mul(amp_t a, amp_t b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__device__ __forceinline__ amp_t c_scale(amp_t a, double t) { return make_double2(a.x * t, a.y * t); }
+__host__ __device__ __forceinline__ amp_t c_scale(amp_t a, double t) { return make_double2(a.x * t, a.y * t); }
 
 // `rotate(z, q)`: z * i^q (src/math/mod.rs:40-50).
-__device__ __forceinline__ amp_t rotate(amp_t z, uint64_t q) {
+__host__ __device__ __forceinline__ amp_t rotate(amp_t z, uint64_t q) {
     if (q & 2) z = c_neg(z);
     if (q & 1) z = make_double2(-z.y, z.x);
     return z;
@@ -27,10 +28,10 @@ __device__ __forceinline__ amp_t rotate(amp_t z, uint64_t q) {
 
 constexpr double kFrac1Sqrt2 = 0.70710678118654752440084436210484903;
 
-__device__ __forceinline__ amp_t gate_m(const DevGate& g, int k) { return make_double2(g.m[2 * k], g.m[2 * k + 1]); }
+__host__ __device__ __forceinline__ amp_t gate_m(const DevGate& g, int k) { return make_double2(g.m[2 * k], g.m[2 * k + 1]); }
 
 template <class Psi>
-__device__ __forceinline__ amp_t atomic_op(const DevGate& g, uint64_t idx, Psi&& psi) {
+__host__ __device__ __forceinline__ amp_t atomic_op(const DevGate& g, uint64_t idx, Psi&& psi) {
     const uint64_t a = g.a;
     switch (g.kind) {
     case QVNT_GATE_X:  // x.rs:15-17

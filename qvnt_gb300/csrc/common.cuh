@@ -43,7 +43,13 @@ __host__ __device__ inline uint64_t enum_index(const Enum& e, uint64_t j) {
     return j | e.ones;
 }
 
-__device__ __forceinline__ unsigned popc64(uint64_t x) { return (unsigned)__popcll(x); }
+__host__ __device__ __forceinline__ unsigned popc64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+    return (unsigned)__popcll(x);
+#else
+    return (unsigned)__builtin_popcountll(x);
+#endif
+}
 
 // Launch geometry: grid sized in multiples of the SM count (152 on GB300).
 struct Geometry {

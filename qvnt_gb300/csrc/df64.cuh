@@ -142,8 +142,9 @@ __host__ __device__ __forceinline__ df df_from_double(double x) {
 
 __host__ __device__ __forceinline__ double df_to_double(df a) { return (double)a.h + (double)a.l; }
 
-// ---- amplitude accessors: register-wide kernels are written once for both storage formats ------
-// Storage is 16 bytes per amplitude in both formats; the pointer is passed as double2*.
+// ---- amplitude accessors: register-wide kernels are written once for every storage format ------
+// Storage is 16 bytes per amplitude for F64 and DF64, 8 bytes (complex<f32>) for C32; the pointer
+// is passed as double2* and each accessor indexes its own element size.
 struct AccF64 {
     static __device__ __forceinline__ double2 load(const double2* p, uint64_t i) { return p[i]; }
     static __device__ __forceinline__ void store(double2* p, uint64_t i, double2 v) { p[i] = v; }
@@ -157,6 +158,16 @@ struct AccDF64 {
     static __device__ __forceinline__ void store(double2* p, uint64_t i, double2 v) {
         const df r = df_from_double(v.x), m = df_from_double(v.y);
         reinterpret_cast<float4*>(p)[i] = make_float4(r.h, r.l, m.h, m.l);
+    }
+};
+
+struct AccC32 {
+    static __device__ __forceinline__ double2 load(const double2* p, uint64_t i) {
+        const float2 v = reinterpret_cast<const float2*>(p)[i];
+        return make_double2((double)v.x, (double)v.y);
+    }
+    static __device__ __forceinline__ void store(double2* p, uint64_t i, double2 v) {
+        reinterpret_cast<float2*>(p)[i] = make_float2((float)v.x, (float)v.y);
     }
 };
 

@@ -71,5 +71,7 @@ int timing_begin(qvnt_reg* r, cudaEvent_t* stop);
 int timing_end(qvnt_reg* r, cudaEvent_t stop);
 int apply_plain(qvnt_reg* r, const qvnt_gate* gates, size_t count);
 int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count);
+int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count);
+int precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* blocks);
 int launch_inv(const double* d_abs, double* d_inv, int* d_status, cudaStream_t stream);
 }  // namespace qvnt

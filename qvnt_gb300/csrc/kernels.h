@@ -1,13 +1,15 @@
 // Host-side launch functions of the engine's kernels.  All run asynchronously on `stream`.
-// `fmt` is the register's storage format: FMT_F64 (IEEE f64, plain engine) or FMT_DF64
-// (double-float pairs, fused engine).  The state pointer is 16 bytes per amplitude in both.
+// `fmt` is the register's storage format: FMT_F64 (IEEE f64, plain engine), FMT_DF64 (double-float
+// pairs, fused engine), both 16 bytes per amplitude, or FMT_C32 (complex<f32>, 8 bytes, precision
+// engine).
 #pragma once
 
 #include "common.cuh"
 
 namespace qvnt {
 
-enum Fmt { FMT_F64 = 0, FMT_DF64 = 1 };
+enum Fmt { FMT_F64 = 0, FMT_DF64 = 1, FMT_C32 = 2 };
+inline uint64_t fmt_bytes(int fmt) { return fmt == FMT_C32 ? 8 : 16; }
 
 // ---- per-gate passes (gates_plain.cu) ----
 bool plain_gate_is_identity(const DevGate& g);
@@ -50,5 +52,13 @@ int launch_tensor(const double2* a, int fa, uint32_t na, const double2* b, int f
                   uint64_t out_len, cudaStream_t stream);
 // In-place storage conversion: to_df != 0: f64 -> df64, else df64 -> f64.
 int launch_convert(double2* psi, uint64_t len, int to_df, cudaStream_t stream);
+// Out-of-place conversion between any two formats (dst may not alias src).
+int launch_convert_fmt(const double2* src, int fsrc, double2* dst, int fdst, uint64_t len, cudaStream_t stream);
+// psi *= sqrt(*d_target / *d_current) (restores a norm after rounding drift; nothing when either is 0).
+int launch_rescale(double2* psi, int fmt, uint64_t len, const double* d_target, const double* d_current,
+                   cudaStream_t stream);
+// <a|b> (re, im), <a|a>, <b|b> and max_i |a_i - b_i| into d_out[0..4]; scratch: 5 * chunk_count(len).
+int launch_overlap(const double2* a, int fa, const double2* b, int fb, uint64_t len, double* scratch, double* d_out,
+                   cudaStream_t stream);
 
 }  // namespace qvnt

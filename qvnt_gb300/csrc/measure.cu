@@ -280,6 +280,82 @@ __global__ void tensor_kernel(const double2* __restrict__ a, uint32_t na, const 
                                        : make_double2(0.0, 0.0));
 }
 
+template <class AccS, class AccD>
+__global__ void convert_fmt_kernel(const double2* __restrict__ src, double2* __restrict__ dst, uint64_t len) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        AccD::store(dst, i, AccS::load(src, i));
+}
+
+template <class Acc>
+__global__ void rescale_kernel(double2* __restrict__ psi, uint64_t len, const double* __restrict__ d_target,
+                               const double* __restrict__ d_current) {
+    const double tgt = *d_target, cur = *d_current;
+    if (!(tgt > 0.0) || !(cur > 0.0)) return;
+    const double f = sqrt(tgt / cur);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride) {
+        const double2 v = Acc::load(psi, i);
+        Acc::store(psi, i, make_double2(v.x * f, v.y * f));
+    }
+}
+
+// Chunk partials of <a|b> = sum conj(a_i) b_i, |a|^2, |b|^2 and max |a_i - b_i|.
+template <class AccA, class AccB>
+__global__ void __launch_bounds__(kRedThreads) overlap_chunk_kernel(const double2* __restrict__ a,
+                                                                     const double2* __restrict__ b, uint64_t len,
+                                                                     double* __restrict__ part) {
+    __shared__ double sm[32];
+    const uint64_t base = (uint64_t)blockIdx.x * kChunk;
+    const uint64_t nc = gridDim.x;
+    double re = 0.0, im = 0.0, na = 0.0, nb = 0.0, mx = 0.0;
+    for (uint32_t k = threadIdx.x; k < kChunk; k += kRedThreads) {
+        const uint64_t i = base + k;
+        if (i >= len) break;
+        const double2 x = AccA::load(a, i), y = AccB::load(b, i);
+        re += x.x * y.x + x.y * y.y;
+        im += x.x * y.y - x.y * y.x;
+        na += nsq(x);
+        nb += nsq(y);
+        mx = fmax(mx, hypot(x.x - y.x, x.y - y.y));
+    }
+    const double r0 = block_sum<kRedThreads>(re, sm);
+    const double r1 = block_sum<kRedThreads>(im, sm);
+    const double r2 = block_sum<kRedThreads>(na, sm);
+    const double r3 = block_sum<kRedThreads>(nb, sm);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int w = 0; w < kRedThreads / 32; ++w) m = fmax(m, sm[w]);
+        part[blockIdx.x] = r0;
+        part[nc + blockIdx.x] = r1;
+        part[2 * nc + blockIdx.x] = r2;
+        part[3 * nc + blockIdx.x] = r3;
+        part[4 * nc + blockIdx.x] = m;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) overlap_final_kernel(const double* __restrict__ part, uint64_t nc,
+                                                                      double* __restrict__ out) {
+    __shared__ double sm[32];
+    for (int q = 0; q < 4; ++q) {
+        double s = 0.0;
+        for (uint64_t k = threadIdx.x; k < nc; k += kScanThreads) s += part[q * nc + k];
+        const double t = block_sum<kScanThreads>(s, sm);
+        if (threadIdx.x == 0) out[q] = t;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (uint64_t k = 0; k < nc; ++k) m = fmax(m, part[4 * nc + k]);
+        out[4] = m;
+    }
+}
+
 // Storage conversion in place: f64 -> df64 (to_df = 1) or df64 -> f64 (to_df = 0).
 __global__ void convert_kernel(double2* __restrict__ psi, uint64_t len, int to_df) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -300,10 +376,11 @@ unsigned flat_grid(uint64_t n) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-#define QVNT_BY_FMT(fmt, KERNEL, ...)                 \
-    do {                                              \
-        if ((fmt) == FMT_DF64) KERNEL<AccDF64> __VA_ARGS__; \
-        else KERNEL<AccF64> __VA_ARGS__;              \
+#define QVNT_BY_FMT(fmt, KERNEL, ...)                          \
+    do {                                                       \
+        if ((fmt) == FMT_DF64) KERNEL<AccDF64> __VA_ARGS__;    \
+        else if ((fmt) == FMT_C32) KERNEL<AccC32> __VA_ARGS__; \
+        else KERNEL<AccF64> __VA_ARGS__;                       \
     } while (0)
 
 }  // namespace
@@ -408,6 +485,49 @@ int launch_tensor(const double2* a, int fa, uint32_t na, const double2* b, int f
 
 int launch_convert(double2* psi, uint64_t len, int to_df, cudaStream_t stream) {
     convert_kernel<<<flat_grid(len), 256, 0, stream>>>(psi, len, to_df);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+namespace {
+template <class AccS>
+void convert_from(const double2* src, double2* dst, int fdst, uint64_t len, cudaStream_t stream) {
+    const unsigned g = flat_grid(len);
+    if (fdst == FMT_DF64) convert_fmt_kernel<AccS, AccDF64><<<g, 256, 0, stream>>>(src, dst, len);
+    else if (fdst == FMT_C32) convert_fmt_kernel<AccS, AccC32><<<g, 256, 0, stream>>>(src, dst, len);
+    else convert_fmt_kernel<AccS, AccF64><<<g, 256, 0, stream>>>(src, dst, len);
+}
+
+template <class AccA>
+void overlap_with(const double2* a, const double2* b, int fb, uint64_t len, double* part, cudaStream_t stream) {
+    const unsigned nc = (unsigned)chunk_count(len);
+    if (fb == FMT_DF64) overlap_chunk_kernel<AccA, AccDF64><<<nc, kRedThreads, 0, stream>>>(a, b, len, part);
+    else if (fb == FMT_C32) overlap_chunk_kernel<AccA, AccC32><<<nc, kRedThreads, 0, stream>>>(a, b, len, part);
+    else overlap_chunk_kernel<AccA, AccF64><<<nc, kRedThreads, 0, stream>>>(a, b, len, part);
+}
+}  // namespace
+
+int launch_convert_fmt(const double2* src, int fsrc, double2* dst, int fdst, uint64_t len, cudaStream_t stream) {
+    if (fsrc == FMT_DF64) convert_from<AccDF64>(src, dst, fdst, len, stream);
+    else if (fsrc == FMT_C32) convert_from<AccC32>(src, dst, fdst, len, stream);
+    else convert_from<AccF64>(src, dst, fdst, len, stream);
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_rescale(double2* psi, int fmt, uint64_t len, const double* d_target, const double* d_current,
+                   cudaStream_t stream) {
+    QVNT_BY_FMT(fmt, rescale_kernel, <<<flat_grid(len), 256, 0, stream>>>(psi, len, d_target, d_current));
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_overlap(const double2* a, int fa, const double2* b, int fb, uint64_t len, double* scratch, double* d_out,
+                   cudaStream_t stream) {
+    if (fa == FMT_DF64) overlap_with<AccDF64>(a, b, fb, len, scratch, stream);
+    else if (fa == FMT_C32) overlap_with<AccC32>(a, b, fb, len, scratch, stream);
+    else overlap_with<AccF64>(a, b, fb, len, scratch, stream);
+    overlap_final_kernel<<<1, kScanThreads, 0, stream>>>(scratch, chunk_count(len), d_out);
     QVNT_CUDA_TRY(cudaGetLastError());
     return QVNT_OK;
 }

@@ -1,0 +1,640 @@
+// Precision engine: complex<f32> amplitudes; runs of gates fused into dense 5-qubit blocks (32 x 32
+// complex unitaries) contracted on the tcgen05 tensor cores.
+//
+// The host lowers every qvnt gate to its dense matrix on its support (targets and controls, split
+// into one-qubit factors for the multi-bit X/Y/Z/S/T of src/operator/atomic/{x,y,z,s,t}.rs), then
+// greedily fuses gates into BLOCKS of at most five qubits (a gate may overtake earlier skipped
+// gates only when their supports are disjoint), multiplying their matrices in double precision.
+// Blocks are grouped into PASSES: a pass picks 12 tile qubits (the 5 lowest, so a tile is a set of
+// 256-byte runs, plus the qubits of up to kMaxPB blocks) and each CTA, persistent over tiles:
+//   1. stages the tile (4096 amplitudes, 32 KB) into shared memory with TMA bulk copies;
+//   2. per block: threads repack the tile into the MMA operand A (128 rows = the 7 other tile bits,
+//      64 columns = the block's 32 amplitudes as (re, im)), split into TF32 hi and lo parts;
+//      one thread issues D = A_lo W_hi^T + A_hi W_lo^T + A_hi W_hi^T as 24 tcgen05.mma (kind::tf32,
+//      M = 128, N = 64, K = 8) into a 128 x 64 FP32 accumulator in tensor memory, where W is the
+//      block's unitary as a real 64 x 64 matrix ([[Re, -Im], [Im, Re]] interleaved), kept in shared
+//      memory for the whole pass; threads read D back with tcgen05.ld and scatter it into the tile;
+//   3. writes the tile back with TMA bulk stores.
+// The three-term TF32 split keeps each block product at ~2^-21 relative error with FP32
+// accumulation.  Every kRenormEvery passes the state is rescaled in FP64 to the norm it had when
+// the apply call started (gates are unitary; this removes FP32 drift and keeps qvnt's unnormalised
+// states unnormalised).  Norms, probabilities and measurement run in FP64 (measure.cu).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "atomic.cuh"
+#include "engine.h"
+#include "kernels.h"
+
+#define TRY_LAUNCH(expr)        \
+    do {                        \
+        const int _s = (expr);  \
+        if (_s) return _s;      \
+    } while (0)
+
+namespace qvnt {
+
+namespace {
+
+constexpr int kPT = 12;            // tile qubits
+constexpr int kBQ = 5;             // block qubits
+constexpr int kBD = 1 << kBQ;      // block dimension
+constexpr int kNT = 256;           // threads: 8 warps, two per tensor-memory lane quadrant
+constexpr int kMaxPB = 3;          // blocks per pass (their weights stay in shared memory)
+constexpr int kRenormEvery = 10;   // passes between FP64 norm restorations
+constexpr uint32_t kPWaitLimit = 1u << 22;
+constexpr uint32_t kTmemCols = 64;
+constexpr uint32_t kWFloats = 64 * 64;  // one weight matrix (hi or lo)
+constexpr size_t kSmemTile = 32768, kSmemA = 32768, kSmemW = 2 * kWFloats * 4;
+
+// Operand layout of tcgen05 for a K-major matrix without swizzling: core matrices of 8 rows x 16
+// bytes (row stride 16 B); the 16 core matrices along K (64 floats) of an 8-row group are contiguous
+// (leading-dimension byte offset 128 B), and the groups follow each other (stride 2048 B).
+__host__ __device__ constexpr uint32_t op_off(uint32_t row, uint32_t k) {
+    return (row >> 3) * 512u + (k >> 2) * 32u + (row & 7u) * 4u + (k & 3u);
+}
+
+struct PBlockDesc {
+    uint8_t bits[kBQ];  // tile-local bit of block bit j
+    uint8_t pad[3];
+    uint32_t w_off;     // float offset of the block's weights (hi, then lo) in the weight buffer
+};
+
+struct PPassParams {
+    uint64_t ntiles;
+    uint32_t k, c, nblocks, pad;
+    uint32_t tq[kPT];
+    PBlockDesc blocks[kMaxPB];
+};
+
+// ---- PTX helpers ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kPWaitLimit; ++it)
+        if (mbar_try(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: start address, LBO = 128 B, SBO = 2048 B, descriptor version 1,
+// no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(2048u >> 4) << 32) |
+           (1ull << 46);
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, A and B TF32 and K-major, N = 64, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+// 32 consecutive accumulator columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__global__ void __launch_bounds__(kNT, 1)
+    precision_tc_kernel(float2* __restrict__ psi, const float* __restrict__ wts, const __grid_constant__ PPassParams P,
+                        int* __restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float2* tile = reinterpret_cast<float2*>(smem);
+    float* a_hi = reinterpret_cast<float*>(smem + kSmemTile);
+    float* a_lo = reinterpret_cast<float*>(smem + kSmemTile + kSmemA);
+    float* w_sm = reinterpret_cast<float*>(smem + kSmemTile + 2 * kSmemA);
+    __shared__ uint64_t seg_off[1 << (kPT - kBQ)];
+    __shared__ uint32_t mpos[kMaxPB][128];
+    __shared__ uint32_t rpos[kMaxPB][kBD];
+    __shared__ __align__(8) uint64_t bar_tma;
+    __shared__ __align__(8) uint64_t bar_mma;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_abort;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t k = P.k, c = P.c, nb = P.nblocks;
+    const uint32_t nseg = 1u << (k - c);
+    const uint32_t seg_amps = 1u << c;
+
+    for (uint32_t s = tid; s < nseg; s += kNT) {
+        uint64_t off = 0;
+        for (uint32_t j = 0; j < k - c; ++j)
+            if ((s >> j) & 1u) off |= 1ull << P.tq[c + j];
+        seg_off[s] = off;
+    }
+    for (uint32_t b = 0; b < nb; ++b) {
+        uint32_t bm = 0;
+        for (int j = 0; j < kBQ; ++j) bm |= 1u << P.blocks[b].bits[j];
+        if (tid < 128) {  // the 7 other tile bits carry the operand row m
+            uint32_t pos = 0, bit = 0;
+            for (uint32_t p = 0; p < (uint32_t)kPT; ++p) {
+                if ((bm >> p) & 1u) continue;
+                if ((tid >> bit) & 1u) pos |= 1u << p;
+                ++bit;
+            }
+            mpos[b][tid] = pos;
+        }
+        if (tid < (uint32_t)kBD) {
+            uint32_t pos = 0;
+            for (int j = 0; j < kBQ; ++j)
+                if ((tid >> j) & 1u) pos |= 1u << P.blocks[b].bits[j];
+            rpos[b][tid] = pos;
+        }
+        const float4* src = reinterpret_cast<const float4*>(wts + P.blocks[b].w_off);
+        float4* dst = reinterpret_cast<float4*>(w_sm + (size_t)b * 2 * kWFloats);
+        for (uint32_t i = tid; i < 2 * kWFloats / 4; i += kNT) dst[i] = __ldg(src + i);
+    }
+    if (warp == 0) {
+        tmem_alloc(&tmem_base, kTmemCols);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        mbar_init(&bar_tma, 1);
+        mbar_init(&bar_mma, 1);
+        fence_mbar_init();
+        s_abort = 0;
+    }
+    fence_proxy_async();  // the weights written above are read by the tensor cores
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = tmem_base;
+    uint32_t ph_tma = 0, ph_mma = 0;
+    for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
+        uint64_t base = t;
+        for (uint32_t p = 0; p < k; ++p) {
+            const uint32_t q = P.tq[p];
+            base = ((base >> q) << (q + 1)) | (base & ((1ull << q) - 1ull));
+        }
+        if (warp == 0) {
+            if (lane == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(&bar_tma, (1u << k) * 8u);
+            }
+            __syncwarp();
+            for (uint32_t s = lane; s < nseg; s += 32)
+                bulk_load(tile + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 8u, &bar_tma);
+        }
+        if (!mbar_wait(&bar_tma, ph_tma)) {
+            atomicExch(err, 1);
+            s_abort = 1;
+        }
+        ph_tma ^= 1u;
+        __syncthreads();
+        if (s_abort) break;
+        for (uint32_t b = 0; b < nb; ++b) {
+            // A[m][2r + c] = component c of the tile amplitude (m, r), split into TF32 hi and lo
+            for (uint32_t i = tid; i < 4096u; i += kNT) {
+                const uint32_t m = i & 127u, r = i >> 7;
+                const float2 x = tile[mpos[b][m] + rpos[b][r]];
+                const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
+                const uint32_t o = op_off(m, 2 * r);
+                *reinterpret_cast<float2*>(a_hi + o) = make_float2(hr, hm);
+                *reinterpret_cast<float2*>(a_lo + o) = make_float2(x.x - hr, x.y - hm);
+            }
+            fence_proxy_async();
+            tc_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc_after_sync();
+                const uint32_t ah = smem_addr(a_hi), al = smem_addr(a_lo);
+                const uint32_t wh = smem_addr(w_sm + (size_t)b * 2 * kWFloats), wl = wh + kWFloats * 4;
+                const uint32_t as[3] = {al, ah, ah};
+                const uint32_t bs[3] = {wh, wl, wh};
+                uint32_t acc = 0;
+                for (int term = 0; term < 3; ++term)
+#pragma unroll
+                    for (uint32_t ks = 0; ks < 8; ++ks) {
+                        mma_tf32(tmem, smem_desc(as[term] + ks * 256u), smem_desc(bs[term] + ks * 256u), acc);
+                        acc = 1;
+                    }
+                mma_commit(&bar_mma);
+            }
+            if (!mbar_wait(&bar_mma, ph_mma)) {
+                atomicExch(err, 1);
+                s_abort = 1;
+            }
+            ph_mma ^= 1u;
+            tc_after_sync();
+            // warp w: accumulator lanes 32 (w % 4) .. + 31 (rows m), columns 32 (w / 4) .. + 31
+            uint32_t v[32];
+            tmem_ld32(tmem + ((32u * (warp & 3u)) << 16) + 32u * (warp >> 2), v);
+            tmem_ld_wait();
+            const uint32_t m = 32u * (warp & 3u) + lane;
+            const uint32_t mp = mpos[b][m];
+#pragma unroll
+            for (uint32_t j = 0; j < 16; ++j)
+                tile[mp + rpos[b][16u * (warp >> 2) + j]] = make_float2(__uint_as_float(v[2 * j]),
+                                                                        __uint_as_float(v[2 * j + 1]));
+            tc_before_sync();
+            __syncthreads();
+            if (s_abort) break;
+        }
+        if (s_abort) break;
+        fence_proxy_async();
+        __syncthreads();
+        if (warp == 0) {
+            for (uint32_t s = lane; s < nseg; s += 32)
+                bulk_store(psi + (base | seg_off[s]), tile + (size_t)s * seg_amps, seg_amps * 8u);
+            bulk_commit();
+            bulk_wait_read();
+        }
+        __syncthreads();
+    }
+    if (s_abort) {
+        // copies or MMAs may still be in flight: wait for both barriers once more (bounded)
+        mbar_wait(&bar_tma, ph_tma);
+        mbar_wait(&bar_mma, ph_mma);
+    }
+    if (warp == 0) bulk_wait_all();
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+// ---- host: dense gate matrices, blocks, passes ----------------------------------------------------
+struct Cd {
+    double re, im;
+};
+inline Cd cmul(Cd a, Cd b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+inline Cd cadd(Cd a, Cd b) { return {a.re + b.re, a.im + b.im}; }
+
+inline uint64_t compress(uint64_t x, const std::vector<int>& sup) {  // global mask -> local bits
+    uint64_t r = 0;
+    for (size_t j = 0; j < sup.size(); ++j)
+        if ((x >> sup[j]) & 1ull) r |= 1ull << j;
+    return r;
+}
+
+struct LGate {
+    uint64_t sup = 0;     // global support mask (<= 5 bits)
+    std::vector<Cd> m;    // dense matrix over the support's local basis, row-major
+};
+
+// The dense matrix of one gate on its support, from qvnt's own atomic formulas (atomic.cuh) and the
+// control rule of dispatch.rs:32-47 (out[i] = f(psi, i) where i has every control bit, else psi[i]).
+int dense_gate(const qvnt_gate& g, LGate& out) {
+    uint64_t tg = g.a_mask;
+    if (g.kind == QVNT_GATE_H2 || g.kind == QVNT_GATE_U2) tg |= g.b_mask;
+    out.sup = tg | g.ctrl;
+    std::vector<int> sup;
+    for (int q = 0; q < 64; ++q)
+        if ((out.sup >> q) & 1ull) sup.push_back(q);
+    if (sup.size() > (size_t)kBQ)
+        return set_error(QVNT_ERR_UNSUPPORTED, "gate acts on %zu qubits (targets and controls); the precision engine "
+                                               "fuses at most %d", sup.size(), kBQ);
+    qvnt_gate lg = g;
+    lg.a_mask = compress(g.a_mask, sup);
+    lg.b_mask = compress(g.b_mask, sup);
+    lg.ctrl = compress(g.ctrl, sup);
+    const DevGate d = decode_gate(lg);
+    const uint64_t dim = 1ull << sup.size();
+    out.m.assign(dim * dim, Cd{0, 0});
+    std::vector<double2> col(dim);
+    for (uint64_t cidx = 0; cidx < dim; ++cidx) {
+        for (uint64_t i = 0; i < dim; ++i) col[i] = make_double2(i == cidx ? 1.0 : 0.0, 0.0);
+        auto psi = [&](uint64_t j) { return col[j]; };
+        for (uint64_t r = 0; r < dim; ++r) {
+            const double2 v = ((r & lg.ctrl) == lg.ctrl) ? atomic_op(d, r, psi) : col[r];
+            out.m[r * dim + cidx] = Cd{v.x, v.y};
+        }
+    }
+    return QVNT_OK;
+}
+
+// Gates as dense factors: the multi-bit X/Y/Z/S/T split into one-qubit factors (they commute), each
+// with the gate's controls.
+int lower_dense(const qvnt_gate* gates, size_t count, std::vector<LGate>& out) {
+    out.clear();
+    for (size_t i = 0; i < count; ++i) {
+        const qvnt_gate& g = gates[i];
+        if (g.kind == QVNT_GATE_ID) continue;
+        const bool multi = g.kind == QVNT_GATE_X || g.kind == QVNT_GATE_Y || g.kind == QVNT_GATE_Z ||
+                           g.kind == QVNT_GATE_S || g.kind == QVNT_GATE_T;
+        if (multi && __builtin_popcountll(g.a_mask) > 1) {
+            for (int q = 0; q < 64; ++q)
+                if ((g.a_mask >> q) & 1ull) {
+                    qvnt_gate f = g;
+                    f.a_mask = 1ull << q;
+                    LGate lg;
+                    const int st = dense_gate(f, lg);
+                    if (st) return set_error(st, "gate %zu: %s", i, qvnt_last_error());
+                    out.push_back(std::move(lg));
+                }
+            continue;
+        }
+        LGate lg;
+        const int st = dense_gate(g, lg);
+        if (st) return set_error(st, "gate %zu: %s", i, qvnt_last_error());
+        out.push_back(std::move(lg));
+    }
+    return QVNT_OK;
+}
+
+struct Block {
+    uint64_t sup = 0;        // exactly kBQ qubits
+    std::vector<Cd> u;       // 32 x 32, row-major, local bit j = j-th qubit of sup (ascending)
+};
+
+// U <- (M on the sub-support) * U, for a gate whose support lies inside the block's.
+void block_apply(Block& b, const LGate& g) {
+    std::vector<int> bq;
+    for (int q = 0; q < 64; ++q)
+        if ((b.sup >> q) & 1ull) bq.push_back(q);
+    std::vector<uint32_t> pos;  // local block bit of each gate-support qubit
+    for (int q = 0; q < 64; ++q)
+        if ((g.sup >> q) & 1ull) pos.push_back((uint32_t)(std::find(bq.begin(), bq.end(), q) - bq.begin()));
+    const uint32_t s = (uint32_t)pos.size(), dim = 1u << s;
+    uint32_t gm = 0;
+    for (uint32_t p : pos) gm |= 1u << p;
+    std::vector<uint32_t> dep(dim);
+    for (uint32_t x = 0; x < dim; ++x) {
+        uint32_t v = 0;
+        for (uint32_t j = 0; j < s; ++j)
+            if ((x >> j) & 1u) v |= 1u << pos[j];
+        dep[x] = v;
+    }
+    std::vector<Cd> tmp(dim);
+    for (uint32_t col = 0; col < (uint32_t)kBD; ++col)
+        for (uint32_t rest = 0; rest < (uint32_t)kBD; ++rest) {
+            if (rest & gm) continue;
+            for (uint32_t r = 0; r < dim; ++r) {
+                Cd acc{0, 0};
+                for (uint32_t cc = 0; cc < dim; ++cc)
+                    acc = cadd(acc, cmul(g.m[r * dim + cc], b.u[(rest | dep[cc]) * kBD + col]));
+                tmp[r] = acc;
+            }
+            for (uint32_t r = 0; r < dim; ++r) b.u[(rest | dep[r]) * kBD + col] = tmp[r];
+        }
+}
+
+void make_blocks(const std::vector<LGate>& lg, uint32_t L, std::vector<Block>& blocks) {
+    blocks.clear();
+    const size_t n = lg.size();
+    std::vector<char> done(n, 0);
+    size_t first = 0;
+    const uint64_t all = L >= 64 ? ~0ull : ((1ull << L) - 1ull);
+    while (true) {
+        while (first < n && done[first]) ++first;
+        if (first >= n) break;
+        uint64_t S = 0, blocked = 0;
+        std::vector<size_t> members;
+        size_t scanned = 0;
+        for (size_t j = first; j < n && scanned < 512; ++j) {
+            if (done[j]) continue;
+            ++scanned;
+            const uint64_t G = lg[j].sup;
+            if (!(G & blocked) && __builtin_popcountll(S | G) <= kBQ) {
+                S |= G;
+                members.push_back(j);
+                done[j] = 1;
+            } else {
+                blocked |= G;
+                if ((blocked & all) == all) break;
+            }
+        }
+        for (int q = 0; q < (int)L && __builtin_popcountll(S) < kBQ; ++q) S |= 1ull << q;  // pad to 5 qubits
+        Block b;
+        b.sup = S;
+        b.u.assign(kBD * kBD, Cd{0, 0});
+        for (int i = 0; i < kBD; ++i) b.u[i * kBD + i] = Cd{1, 0};
+        for (size_t j : members) block_apply(b, lg[j]);
+        blocks.push_back(std::move(b));
+    }
+}
+
+struct PPlan {
+    uint64_t qmask;
+    std::vector<size_t> members;  // block indices
+};
+
+void make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan>& passes) {
+    passes.clear();
+    const size_t n = blocks.size();
+    std::vector<char> done(n, 0);
+    size_t first = 0;
+    const uint64_t low = (1ull << kBQ) - 1ull;
+    while (true) {
+        while (first < n && done[first]) ++first;
+        if (first >= n) break;
+        PPlan p;
+        uint64_t Q = low, blocked = 0;
+        size_t scanned = 0;
+        for (size_t j = first; j < n && scanned < 64 && p.members.size() < (size_t)kMaxPB; ++j) {
+            if (done[j]) continue;
+            ++scanned;
+            const uint64_t S = blocks[j].sup;
+            if (!(S & blocked) && __builtin_popcountll(Q | S) <= kPT) {
+                Q |= S;
+                p.members.push_back(j);
+                done[j] = 1;
+            } else {
+                blocked |= S;
+            }
+        }
+        for (uint32_t q = 0; q < L && __builtin_popcountll(Q) < kPT; ++q) Q |= 1ull << q;
+        p.qmask = Q;
+        passes.push_back(std::move(p));
+    }
+}
+
+// TF32 rounding to nearest (ties away from zero), as cvt.rna.tf32.f32 does on the device.
+float tf32_host(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) != 0x7f800000u) {
+        u += 0x1000u;
+        u &= 0xffffe000u;
+    }
+    float r;
+    memcpy(&r, &u, 4);
+    return r;
+}
+
+// Weights of a block in the operand layout: W[2r' + c'][2r + c] = ((Re, -Im), (Im, Re)) of U[r'][r];
+// hi = TF32(W), lo = W - hi.
+void block_weights(const Block& b, float* hi, float* lo) {
+    for (uint32_t rp = 0; rp < (uint32_t)kBD; ++rp)
+        for (uint32_t r = 0; r < (uint32_t)kBD; ++r) {
+            const Cd u = b.u[rp * kBD + r];
+            const float w[2][2] = {{(float)u.re, (float)-u.im}, {(float)u.im, (float)u.re}};
+            for (int cp = 0; cp < 2; ++cp)
+                for (int cc = 0; cc < 2; ++cc) {
+                    const uint32_t o = op_off(2 * rp + cp, 2 * r + cc);
+                    const float h = tf32_host(w[cp][cc]);
+                    hi[o] = h;
+                    lo[o] = w[cp][cc] - h;
+                }
+        }
+}
+
+}  // namespace
+
+int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
+    const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
+    if (L < (uint32_t)kPT)
+        return set_error(QVNT_ERR_UNSUPPORTED, "the precision engine needs at least %d qubits", kPT);
+    std::vector<LGate> lg;
+    int st = lower_dense(gates, count, lg);
+    if (st) return st;
+    if (lg.empty()) return QVNT_OK;
+    std::vector<Block> blocks;
+    make_blocks(lg, L, blocks);
+    std::vector<PPlan> passes;
+    make_passes(blocks, L, passes);
+    // weights of every block, uploaded once per apply call
+    const size_t wfl = blocks.size() * 2 * kWFloats;
+    FusedState& fs = r->fused;
+    if (fs.h_buf) QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));  // the last upload has left h_buf
+    if (fs.d_bytes < wfl * 4) {
+        fs.release();
+        QVNT_CUDA_TRY(cudaMalloc(&fs.d_buf, wfl * 4));
+        QVNT_CUDA_TRY(cudaMallocHost(&fs.h_buf, wfl * 4));
+        fs.d_bytes = fs.h_bytes = wfl * 4;
+    }
+    float* hw = static_cast<float*>(fs.h_buf);
+    for (size_t i = 0; i < blocks.size(); ++i) block_weights(blocks[i], hw + i * 2 * kWFloats, hw + i * 2 * kWFloats + kWFloats);
+    QVNT_CUDA_TRY(cudaMemcpyAsync(fs.d_buf, fs.h_buf, wfl * 4, cudaMemcpyHostToDevice, r->stream));
+    // the norm to keep (FP64)
+    double* d_norm0 = reinterpret_cast<double*>(r->d_small) + 5;
+    double* d_norm = reinterpret_cast<double*>(r->d_small) + 6;
+    TRY_LAUNCH(launch_norm_sqr_sum(r->psi, r->fmt, r->len, r->scratch, d_norm0, r->stream));
+    static const bool attr = [] {
+        return cudaFuncSetAttribute((const void*)precision_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(kSmemTile + 2 * kSmemA + kMaxPB * kSmemW)) == cudaSuccess;
+    }();
+    if (!attr) return set_error(QVNT_ERR_CUDA, "precision kernel: shared-memory attribute refused");
+    int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
+    PPassParams P;
+    size_t since = 0;
+    for (size_t pi = 0; pi < passes.size(); ++pi) {
+        const PPlan& p = passes[pi];
+        memset(&P, 0, sizeof P);
+        uint32_t n = 0, pos_of[64];
+        for (uint32_t b = 0; b < L; ++b)
+            if ((p.qmask >> b) & 1ull) {
+                pos_of[b] = n;
+                P.tq[n++] = b;
+            }
+        uint32_t run = 0;
+        while (run < n && P.tq[run] == run) ++run;
+        P.k = n;
+        P.c = run;
+        P.ntiles = r->len >> n;
+        P.nblocks = (uint32_t)p.members.size();
+        for (size_t j = 0; j < p.members.size(); ++j) {
+            const Block& b = blocks[p.members[j]];
+            uint32_t jj = 0;
+            for (uint32_t q = 0; q < L; ++q)
+                if ((b.sup >> q) & 1ull) P.blocks[j].bits[jj++] = (uint8_t)pos_of[q];
+            P.blocks[j].w_off = (uint32_t)(p.members[j] * 2 * kWFloats);
+        }
+        const size_t smem = kSmemTile + 2 * kSmemA + P.nblocks * kSmemW;
+        uint64_t grid = (uint64_t)r->ctx->geo.sms;
+        if (grid > P.ntiles) grid = P.ntiles;
+        cudaEvent_t stop = nullptr;
+        st = timing_begin(r, &stop);
+        if (st) return st;
+        precision_tc_kernel<<<(unsigned)grid, kNT, smem, r->stream>>>(reinterpret_cast<float2*>(r->psi),
+                                                                        static_cast<const float*>(fs.d_buf), P, d_err);
+        QVNT_CUDA_TRY(cudaGetLastError());
+        st = timing_end(r, stop);
+        if (st) return st;
+        r->launches += 1;
+        r->passes += 1;
+        if (++since == (size_t)kRenormEvery || pi + 1 == passes.size()) {
+            since = 0;
+            TRY_LAUNCH(launch_norm_sqr_sum(r->psi, r->fmt, r->len, r->scratch, d_norm, r->stream));
+            TRY_LAUNCH(launch_rescale(r->psi, r->fmt, r->len, d_norm0, d_norm, r->stream));
+            r->launches += 3;
+        }
+    }
+    return QVNT_OK;
+}
+
+int precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* blocks) {
+    std::vector<LGate> lg;
+    int st = lower_dense(gates, count, lg);
+    if (st) return st;
+    std::vector<Block> bl;
+    make_blocks(lg, L, bl);
+    std::vector<PPlan> ps;
+    make_passes(bl, L, ps);
+    *passes = ps.size();
+    *blocks = bl.size();
+    return QVNT_OK;
+}
+
+}  // namespace qvnt

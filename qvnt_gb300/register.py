@@ -158,11 +158,12 @@ class QReg:
     def __init__(self, q_num, state=0, ctx=None, engine=None):
         self.ctx = ctx or default_context()
         h = ctypes.c_void_p()
-        check(lib().qvnt_reg_create(self.ctx.h, q_num, state, ctypes.byref(h)))
+        if engine is None:
+            check(lib().qvnt_reg_create(self.ctx.h, q_num, state, ctypes.byref(h)))
+        else:
+            check(lib().qvnt_reg_create_ex(self.ctx.h, q_num, state, engine, ctypes.byref(h)))
         self.h = h
         self.q_num = q_num
-        if engine is not None:
-            self.set_engine(engine)
 
     @classmethod
     def _wrap(cls, h, q_num, ctx):
@@ -247,6 +248,12 @@ class QReg:
         out = np.empty((1 << self.q_num, 2), dtype=np.float64)
         check(lib().qvnt_reg_get_polar(self.h, out.ctypes.data))
         return out
+
+    def overlap(self, other):
+        """(fidelity |<self|other>|^2 / (<self|self> <other|other>), max |self_i - other_i|), in FP64."""
+        f, m = ctypes.c_double(), ctypes.c_double()
+        check(lib().qvnt_reg_overlap(self.h, other.h, ctypes.byref(f), ctypes.byref(m)))
+        return f.value, m.value
 
     def amplitudes(self):
         """All max(2^n, 8) amplitudes (qvnt's `psi` field) as complex128."""
