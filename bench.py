@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1, help="steps of the plain f64 GPU path (0 = skip)")
-    ap.add_argument("--forms", default="batch,serve", help="extra forms to measure: batch, serve (empty = none)")
+    ap.add_argument("--forms", default="batch,serve,precision",
+                    help="extra forms to measure: batch, serve, precision (empty = none)")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
@@ -230,16 +231,80 @@ def bench_batch(ctx, count, steps):
                               % len(sample)}}
 
 
+def bench_precision(ctx, n=32, depth=60, n_ref=30):
+    """Precision form: complex<f32> register of n qubits (32 GiB at 32), the random-layer generator
+    at depth 60, dense 5-qubit blocks on the tensor cores with FP64 norm restoration every 10
+    passes.  Fidelity defect and max-abs error against the double-float engine (f64-equivalent,
+    within 1e-12 of the oracle) at n_ref qubits with the same seed; the plain f64 GPU path at n
+    qubits timed on the first 64 gates and extrapolated per gate."""
+    import torch
+    from qvnt_gb300 import ENGINE_FUSED, ENGINE_PLAIN, ENGINE_PRECISION, QReg
+    from qvnt_gb300.circuits import SplitMix64, random_layers_gates
+
+    def gates(m):
+        return random_layers_gates(m, depth, SplitMix64(3))
+
+    arr, cnt = gates(n)
+    q = QReg(n, 0, ctx=ctx, engine=ENGINE_PRECISION)
+    q.apply_gates(arr, cnt)  # warm-up
+    q.sync()
+    q.kernel_timing(enable=1)
+    s = torch.cuda.ExternalStream(q.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    _, p0 = q.stats()
+    e0.record(s)
+    q.reset(0)
+    q.apply_gates(arr, cnt)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kms, kn = q.kernel_timing(enable=0)
+    _, p1 = q.stats()
+    q.close()
+    del q
+    pass_bytes = 2 * (1 << n) * 8
+    # plain f64 path at the same size, per gate on a sample
+    qp = QReg(n, 0, ctx=ctx, engine=ENGINE_PLAIN)
+    sp = torch.cuda.ExternalStream(qp.stream())
+    sample = min(64, cnt)
+    qp.apply_gates(arr, 4)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(sp)
+    qp.apply_gates(arr, sample)
+    f1.record(sp)
+    torch.cuda.synchronize()
+    plain_ms_per_gate = f0.elapsed_time(f1) / sample
+    qp.close()
+    del qp
+    # fidelity at n_ref qubits against the f64-equivalent engine
+    arr_r, cnt_r = gates(n_ref)
+    a = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_PRECISION)
+    a.apply_gates(arr_r, cnt_r)
+    b = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_FUSED)
+    b.apply_gates(arr_r, cnt_r)
+    fid, mx = a.overlap(b)
+    a.close()
+    b.close()
+    avg = kms / kn
+    return {"workload": "%d qubits complex<f32>, random layers depth %d (%d gates), dense 5-qubit blocks on tcgen05 "
+                        "(TF32 hi/lo, FP32 accumulate), FP64 norm restoration every 10 passes" % (n, depth, cnt),
+            "circuits_per_s": 1e3 / ms, "ms_per_circuit": ms, "gate_passes_per_s": cnt / (ms / 1e3),
+            "passes": p1 - p0, "kernel_avg_ms": avg, "kernel_gbs": pass_bytes / (avg / 1e3) / 1e9,
+            "fidelity_defect_vs_f64": 1.0 - fid, "max_abs_err_vs_f64": mx, "fidelity_qubits": n_ref,
+            "plain_f64_gpu": {"circuits_per_s": 1e3 / (plain_ms_per_gate * cnt),
+                              "sample": "first %d gates at %d qubits, extrapolated per gate" % (sample, n)}}
+
+
 def bench_serve(ctx, rate, seconds):
     """Serving form: Poisson arrivals at `rate`/s for `seconds` s (n log-uniform [10, 28], depth
-    uniform [5, 100] over 1-3 apply/measure rounds, 150 GB HBM budget, 16 slots, queue of 1024);
+    uniform [5, 100] over 1-3 apply/measure rounds, 150 GB HBM budget, 32 slots, queue of 1024);
     then 5 s to drain.  Latency = completion - scheduled arrival."""
     import numpy as np
     from qvnt_gb300.circuits import serve_requests
     from qvnt_gb300.serve import Server
 
     max_queue = 1024
-    s = Server(budget_bytes=150 * 10**9, slots=16, max_queue=max_queue, ctx=ctx)
+    s = Server(budget_bytes=150 * 10**9, slots=32, max_queue=max_queue, ctx=ctx)
     t0 = s.clock()
     offered = shed = 0
     for r in serve_requests(rate=rate, duration=seconds, seed=5):
@@ -262,7 +327,7 @@ def bench_serve(ctx, rate, seconds):
     pct = (lambda a, p: float(np.percentile(a, p)) * 1e3 if a.size else None)
     censored = np.concatenate([lat, ages]) if ages.size else lat
     return {"workload": "Poisson %.0f req/s for %.0f s, n log-uniform [10, 28], depth uniform [5, 100], "
-                        "1-3 apply/measure rounds, 150 GB budget, 16 slots" % (rate, seconds),
+                        "1-3 apply/measure rounds, 150 GB budget, 32 slots, queue 1024" % (rate, seconds),
             "offered": offered, "submitted": st["submitted"], "shed": shed, "completed": st["completed"],
             "failed": st["failed"], "queued_at_end": st["queued"], "running_at_end": st["running"],
             "served_circuits_per_s": st["completed"] / elapsed, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),
@@ -441,6 +506,8 @@ def main():
                     forms["batch"] = bench_batch(ctx, args.batch_count, max(1, args.steps))
                 elif form == "serve":
                     forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds)
+                elif form == "precision":
+                    forms["precision"] = bench_precision(ctx)
             except Exception as exc:  # a form's failure is reported, not hidden
                 forms[form] = {"error": "%s: %s" % (type(exc).__name__, exc)}
 

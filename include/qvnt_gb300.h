@@ -331,9 +331,11 @@ int qvnt_batch_info(const qvnt_batch* batch, uint64_t* items, uint64_t* passes, 
  *
  *   qvnt_server_create   `slots` worker threads; requests are admitted while the states of the
  *                        running ones fit `hbm_budget_bytes` (16 B per amplitude, plus the same again
- *                        for a request that keeps its amplitudes); the first queued request that fits
- *                        goes next, except that a head request older than 0.5 s blocks bypassing.
- *                        Requests beyond `max_queue` queued ones are shed (QVNT_ERR_BUSY; 0 = 4096).
+ *                        for a request that keeps its amplitudes).  Among the queued requests that
+ *                        fit, the one with the least work (amplitudes x gates) discounted by
+ *                        exp(-waiting seconds) goes next; requests of 24 qubits or more hold at most
+ *                        a quarter of the slots.  Requests beyond `max_queue` queued ones are shed
+ *                        (QVNT_ERR_BUSY; 0 = 4096).
  *   qvnt_server_submit   copies the request (gates validated against the register); `arrival_s` is
  *                        its arrival on the server clock (qvnt_server_clock; < 0 = now), the start of
  *                        its latency.  flags: QVNT_SUBMIT_KEEP_AMPLITUDES keeps the final state for

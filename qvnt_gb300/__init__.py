@@ -10,9 +10,10 @@ library's CUDA kernels (qvnt_gb300/csrc/).  This package is the Python side of t
 include/qvnt_gb300.h.
 """
 from . import operator as op
-from ._abi import ENGINE_FUSED, ENGINE_PLAIN, KIND, KINDS, MaskError, QvntError, QvntGate
+from ._abi import ENGINE_FUSED, ENGINE_PLAIN, ENGINE_PRECISION, KIND, KINDS, MaskError, QvntError, QvntGate
 from .operator import MultiOp, SingleOp
 from .register import Context, CReg, QReg, VReg, bits_iter, default_context
 
 __all__ = ["op", "QReg", "CReg", "VReg", "MultiOp", "SingleOp", "Context", "default_context", "bits_iter",
-           "QvntGate", "QvntError", "MaskError", "KIND", "KINDS", "ENGINE_FUSED", "ENGINE_PLAIN"]
+           "QvntGate", "QvntError", "MaskError", "KIND", "KINDS", "ENGINE_FUSED", "ENGINE_PLAIN",
+           "ENGINE_PRECISION"]

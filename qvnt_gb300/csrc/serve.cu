@@ -8,7 +8,8 @@
 // `slots` worker threads each run one request at a time on the request's own CUDA stream, so the
 // kernels of different requests overlap on the device.  A worker that frees up admits, among the
 // queued requests whose state fits the HBM budget next to the running ones, the one with the least
-// estimated work discounted by its waiting time (shortest first, with ageing).
+// estimated work discounted by its waiting time (shortest first, with ageing); requests of 24 qubits
+// or more may hold at most a quarter of the slots.
 // Registers are pooled by size and reused through `qvnt_reg_reset`, so steady-state admission
 // allocates nothing and never hits the device-wide synchronisation of cudaFree; idle pooled
 // registers are freed only when a new size needs their memory.  Streams of small registers get the
@@ -34,6 +35,9 @@ using Clock = std::chrono::steady_clock;
 
 constexpr uint32_t kMagicServer = 0x51535256u;
 constexpr double kAgeScale = 1.0;  // seconds: waiting time that discounts a request's work by e
+// Requests whose state is at least kLargeBytes are "large": at most a quarter of the slots run
+// them at once, so that long requests cannot hold every slot while short ones queue.
+constexpr uint64_t kLargeBytes = 16ull << 24;  // a 24-qubit state
 
 struct Request {
     uint64_t id = 0;
@@ -83,6 +87,7 @@ struct qvnt_server {
     std::vector<qvnt_reg*> to_free;
     // statistics
     uint64_t submitted = 0, shed = 0, completed = 0, failed = 0, running = 0, peak_running = 0;
+    uint64_t large_running = 0;
     std::vector<double> latencies;
     std::vector<std::thread> workers;
 
@@ -103,11 +108,13 @@ int priority_for(const qvnt_server* s, uint32_t n) {
 // after waiting about kAgeScale * ln(work ratio).  Returns queue.end() when none fits.
 std::deque<Request*>::iterator pick(qvnt_server* s) {
     const double t = s->now();
+    const uint64_t max_large = std::max<uint64_t>(1, s->slots / 4);
     auto best = s->queue.end();
     double best_score = 0.0;
     for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
         // idle pooled registers are reused or evicted, so only running requests hold memory
         if (s->bytes_active + (*it)->footprint > s->budget) continue;
+        if ((*it)->footprint >= kLargeBytes && s->large_running >= max_large) continue;
         const double score = (*it)->work * std::exp(-(t - (*it)->arrival) / kAgeScale);
         if (best == s->queue.end() || score < best_score) {
             best = it;
@@ -168,6 +175,8 @@ void worker(qvnt_server* s) {
         }
         s->bytes_active += r->footprint;
         s->running += 1;
+        const bool large = r->footprint >= kLargeBytes;
+        if (large) s->large_running += 1;
         s->peak_running = std::max(s->peak_running, s->running);
         std::vector<qvnt_reg*> frees;
         frees.swap(s->to_free);
@@ -195,6 +204,7 @@ void worker(qvnt_server* s) {
         r->done = true;
         s->bytes_active -= r->footprint;
         s->running -= 1;
+        if (large) s->large_running -= 1;
         if (reg) {
             s->idle.emplace(r->n, std::make_pair(reg, r->footprint));
             s->bytes_idle += r->footprint;
