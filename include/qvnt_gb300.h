@@ -296,7 +296,8 @@ int qvnt_reg_kernel_timing(qvnt_reg* reg, int enable, double* ms, uint64_t* laun
  *   qvnt_batch_set_fusion / qvnt_batch_autotune
  *                       re-plan with a tile width (fusion_k, 6..12) and pass budget (estimated FP32
  *                       instructions per amplitude a pass may hold; 0 = the engine default), or pick
- *                       both by timing the schedule of every stride-th register under each candidate.
+ *                       both, and the kernel's register budget (2 CTAs per SM or 1 without spills), by
+ *                       timing the schedule of every stride-th register under each candidate.
  *   qvnt_batch_get_amplitudes  register `index` after the last run, interleaved (re, im) f64.
  *   qvnt_batch_info     schedule items and passes, state bytes, fusion width, pass budget, and the
  *                       device time of the last run (events around the graph launch).

@@ -888,6 +888,8 @@ __global__ void __launch_bounds__(1 << (KT - KR), MINB) batch_df_kernel(const __
     }
 }
 
+// Two register budgets of the batch kernel: 2 CTAs per SM (128 registers, some spills) or 1 CTA per
+// SM (no spills, half the warps); the autotuner picks one per batch.
 constexpr int kBatchKT = 12, kBatchKR = 4, kBatchMinB = 2;
 
 // ---- kernel configurations ----------------------------------------------------------------------
@@ -1850,6 +1852,7 @@ struct qvnt_batch {
     uint64_t nitems = 0, npasses = 0;
     uint32_t fusion_k = kBatchKT;
     int budget = 0;
+    int minb = kBatchMinB;  // kernel variant: CTAs per SM
     bool has_measure = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1911,13 +1914,19 @@ int batch_upload(qvnt_batch* b, const BatchSchedule& s, void** d_buf, BatchArgs*
     return QVNT_OK;
 }
 
-int batch_grid(qvnt_batch* b, unsigned* grid) {
+using BatchFn = void (*)(BatchArgs);
+
+BatchFn batch_fn(int minb) {
+    return minb == 1 ? batch_df_kernel<kBatchKT, kBatchKR, 1> : batch_df_kernel<kBatchKT, kBatchKR, kBatchMinB>;
+}
+
+int batch_grid(qvnt_batch* b, int minb, unsigned* grid) {
     constexpr size_t smem = ((size_t)1 << kBatchKT) * 16;
-    static std::atomic<bool> attr{false};
-    auto fn = batch_df_kernel<kBatchKT, kBatchKR, kBatchMinB>;
-    if (!attr.load(std::memory_order_acquire)) {
+    static std::atomic<bool> attr[3] = {};
+    const BatchFn fn = batch_fn(minb);
+    if (!attr[minb].load(std::memory_order_acquire)) {
         QVNT_CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr.store(true, std::memory_order_release);
+        attr[minb].store(true, std::memory_order_release);
     }
     int per_sm = 0;
     QVNT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, 1 << (kBatchKT - kBatchKR),
@@ -1929,7 +1938,7 @@ int batch_grid(qvnt_batch* b, unsigned* grid) {
 
 // Enqueues one run: draws in, counters and states reset, the persistent kernel, results out.  No
 // call here may synchronise: the sequence is captured into the batch's CUDA graph.
-int batch_enqueue(qvnt_batch* b, const BatchArgs& A, unsigned grid, cudaStream_t s) {
+int batch_enqueue(qvnt_batch* b, const BatchArgs& A, unsigned grid, int minb, cudaStream_t s) {
     const uint32_t n = (uint32_t)b->regs.size();
     QVNT_CUDA_TRY(cudaMemcpyAsync(b->d_u01, b->h_u01, n * sizeof(double), cudaMemcpyHostToDevice, s));
     QVNT_CUDA_TRY(cudaMemsetAsync(b->d_done, 0, n * sizeof(unsigned int), s));
@@ -1938,8 +1947,11 @@ int batch_enqueue(qvnt_batch* b, const BatchArgs& A, unsigned grid, cudaStream_t
     batch_basis_kernel<<<(n + 255) / 256, 256, 0, s>>>(b->psi, b->d_basis, n);
     QVNT_CUDA_TRY(cudaGetLastError());
     if (A.nitems) {
-        batch_df_kernel<kBatchKT, kBatchKR, kBatchMinB>
-            <<<grid, 1 << (kBatchKT - kBatchKR), ((size_t)1 << kBatchKT) * 16, s>>>(A);
+        if (minb == 1)
+            batch_df_kernel<kBatchKT, kBatchKR, 1><<<grid, 1 << (kBatchKT - kBatchKR), ((size_t)1 << kBatchKT) * 16, s>>>(A);
+        else
+            batch_df_kernel<kBatchKT, kBatchKR, kBatchMinB>
+                <<<grid, 1 << (kBatchKT - kBatchKR), ((size_t)1 << kBatchKT) * 16, s>>>(A);
         QVNT_CUDA_TRY(cudaGetLastError());
     }
     QVNT_CUDA_TRY(cudaMemcpyAsync(b->h_results, b->d_results, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
@@ -1957,7 +1969,7 @@ void batch_drop_schedule(qvnt_batch* b) {
 }
 
 // Plans all registers with (fusion_k, budget), uploads, and captures the run as a CUDA graph.
-int batch_plan(qvnt_batch* b, uint32_t fusion_k, int budget) {
+int batch_plan(qvnt_batch* b, uint32_t fusion_k, int budget, int minb) {
     std::vector<uint32_t> all(b->regs.size());
     for (uint32_t i = 0; i < all.size(); ++i) all[i] = i;
     BatchSchedule s;
@@ -1972,11 +1984,12 @@ int batch_plan(qvnt_batch* b, uint32_t fusion_k, int budget) {
     b->npasses = s.passes.size();
     b->fusion_k = fusion_k;
     b->budget = budget;
+    b->minb = minb;
     unsigned grid = 0;
-    st = batch_grid(b, &grid);
+    st = batch_grid(b, minb, &grid);
     if (st) return st;
     QVNT_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    st = batch_enqueue(b, b->args, grid, b->stream);
+    st = batch_enqueue(b, b->args, grid, minb, b->stream);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (st) {
@@ -2105,7 +2118,7 @@ extern "C" int qvnt_batch_create(qvnt_ctx* ctx, uint32_t count, const uint32_t* 
         return st;
     }
     b->magic = kMagicBatch;
-    const int st = batch_plan(b, kBatchKT, 0);
+    const int st = batch_plan(b, kBatchKT, 0, kBatchMinB);
     if (st) {
         batch_free(b);
         return st;
@@ -2126,7 +2139,7 @@ extern "C" int qvnt_batch_set_fusion(qvnt_batch* b, uint32_t fusion_k, uint32_t 
         return set_error(QVNT_ERR_BAD_ARG, "fusion width %u outside [%u, %d]", fusion_k, kFusedMinK, kBatchKT);
     if (pass_budget > (1u << 20)) return set_error(QVNT_ERR_BAD_ARG, "pass budget %u too large", pass_budget);
     QVNT_CUDA_TRY(cudaSetDevice(b->ctx->device));
-    return batch_plan(b, fusion_k, (int)pass_budget);
+    return batch_plan(b, fusion_k, (int)pass_budget, b->minb);
 }
 
 extern "C" int qvnt_batch_run(qvnt_batch* b, const double* u01, uint64_t* measured) {
@@ -2163,44 +2176,50 @@ extern "C" int qvnt_batch_autotune(qvnt_batch* b, uint32_t stride, uint32_t* fus
     QVNT_CUDA_TRY(cudaSetDevice(b->ctx->device));
     std::vector<uint32_t> sub;
     for (uint32_t i = 0; i < b->regs.size(); i += stride) sub.push_back(i);
-    const uint32_t ks[] = {11, 12};
-    const int budgets[] = {100, 200, 400, 800};
-    unsigned grid = 0;
-    int gst = batch_grid(b, &grid);
-    if (gst) return gst;
+    struct Cand {
+        uint32_t k;
+        int budget, minb;
+    };
+    const Cand cands[] = {{12, 200, 2}, {12, 400, 2}, {12, 800, 2}, {12, 1600, 2},
+                          {12, 400, 1}, {12, 800, 1}, {12, 1600, 1}, {11, 800, 2}};
     double best = 1e300;
     uint32_t bk = kBatchKT;
-    int bb = 0;
-    for (uint32_t k : ks)
-        for (int bud : budgets) {
-            BatchSchedule s;
-            int st = build_batch_schedule(b->regs, sub, k, bud, s);
-            if (st) return st;
-            void* d = nullptr;
-            BatchArgs A{};
-            st = batch_upload(b, s, &d, &A);
-            if (st) return st;
-            float ms = 0.f;
-            st = batch_enqueue(b, A, grid, b->stream);  // warm-up (first touch of the schedule)
-            if (!st) {
-                cudaEventRecord(b->ev0, b->stream);
-                st = batch_enqueue(b, A, grid, b->stream);
-                cudaEventRecord(b->ev1, b->stream);
-            }
-            cudaError_t e = cudaStreamSynchronize(b->stream);
-            cudaFree(d);
-            if (st) return st;
-            if (e != cudaSuccess) return set_cuda_error(e, "batch autotune run");
-            st = batch_check_err(b);
-            if (st) return st;
-            QVNT_CUDA_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-            if (ms < best) {
-                best = ms;
-                bk = k;
-                bb = bud;
-            }
+    int bb = 0, bm = kBatchMinB;
+    for (const Cand& cd : cands) {
+        const uint32_t k = cd.k;
+        const int bud = cd.budget;
+        unsigned grid = 0;
+        int gst = batch_grid(b, cd.minb, &grid);
+        if (gst) return gst;
+        BatchSchedule s;
+        int st = build_batch_schedule(b->regs, sub, k, bud, s);
+        if (st) return st;
+        void* d = nullptr;
+        BatchArgs A{};
+        st = batch_upload(b, s, &d, &A);
+        if (st) return st;
+        float ms = 0.f;
+        st = batch_enqueue(b, A, grid, cd.minb, b->stream);  // warm-up (first touch of the schedule)
+        if (!st) {
+            cudaEventRecord(b->ev0, b->stream);
+            st = batch_enqueue(b, A, grid, cd.minb, b->stream);
+            cudaEventRecord(b->ev1, b->stream);
         }
-    const int st = batch_plan(b, bk, bb);
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        cudaFree(d);
+        if (st) return st;
+        if (e != cudaSuccess) return set_cuda_error(e, "batch autotune run");
+        st = batch_check_err(b);
+        if (st) return st;
+        QVNT_CUDA_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        if (ms < best) {
+            best = ms;
+            bk = k;
+            bb = bud;
+            bm = cd.minb;
+        }
+    }
+    const int st = batch_plan(b, bk, bb, bm);
     if (st) return st;
     if (fusion_k) *fusion_k = bk;
     if (pass_budget) *pass_budget = (uint32_t)bb;

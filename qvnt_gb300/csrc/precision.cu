@@ -7,7 +7,8 @@
 // gates only when their supports are disjoint), multiplying their matrices in double precision.
 // Blocks are grouped into PASSES: a pass picks 12 tile qubits (the 5 lowest, so a tile is a set of
 // 256-byte runs, plus the qubits of up to kMaxPB blocks) and each CTA, persistent over tiles:
-//   1. stages the tile (4096 amplitudes, 32 KB) into shared memory with TMA bulk copies;
+//   1. stages the tile (4096 amplitudes, 32 KB) into shared memory with TMA bulk copies, the next
+//      tile's copies running into a second buffer while this one is processed;
 //   2. per block: threads repack the tile into the MMA operand A (128 rows = the 7 other tile bits,
 //      64 columns = the block's 32 amplitudes as (re, im)), split into TF32 hi and lo parts;
 //      one thread issues D = A_lo W_hi^T + A_hi W_lo^T + A_hi W_hi^T as 24 tcgen05.mma (kind::tf32,
@@ -42,7 +43,7 @@ constexpr int kPT = 12;            // tile qubits
 constexpr int kBQ = 5;             // block qubits
 constexpr int kBD = 1 << kBQ;      // block dimension
 constexpr int kNT = 256;           // threads: 8 warps, two per tensor-memory lane quadrant
-constexpr int kMaxPB = 3;          // blocks per pass (their weights stay in shared memory)
+constexpr int kMaxPB = 2;          // blocks per pass (their weights stay in shared memory)
 constexpr int kRenormEvery = 10;   // passes between FP64 norm restorations
 constexpr uint32_t kPWaitLimit = 1u << 22;
 constexpr uint32_t kTmemCols = 64;
@@ -171,14 +172,15 @@ __global__ void __launch_bounds__(kNT, 1)
     precision_tc_kernel(float2* __restrict__ psi, const float* __restrict__ wts, const __grid_constant__ PPassParams P,
                         int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    float2* tile = reinterpret_cast<float2*>(smem);
-    float* a_hi = reinterpret_cast<float*>(smem + kSmemTile);
-    float* a_lo = reinterpret_cast<float*>(smem + kSmemTile + kSmemA);
-    float* w_sm = reinterpret_cast<float*>(smem + kSmemTile + 2 * kSmemA);
+    // two tile buffers: the next tile's load overlaps the current tile's blocks
+    float2* tiles = reinterpret_cast<float2*>(smem);
+    float* a_hi = reinterpret_cast<float*>(smem + 2 * kSmemTile);
+    float* a_lo = reinterpret_cast<float*>(smem + 2 * kSmemTile + kSmemA);
+    float* w_sm = reinterpret_cast<float*>(smem + 2 * kSmemTile + 2 * kSmemA);
     __shared__ uint64_t seg_off[1 << (kPT - kBQ)];
     __shared__ uint32_t mpos[kMaxPB][128];
     __shared__ uint32_t rpos[kMaxPB][kBD];
-    __shared__ __align__(8) uint64_t bar_tma;
+    __shared__ __align__(8) uint64_t bar_tma[2];
     __shared__ __align__(8) uint64_t bar_mma;
     __shared__ uint32_t tmem_base;
     __shared__ int s_abort;
@@ -220,43 +222,63 @@ __global__ void __launch_bounds__(kNT, 1)
         tmem_relinquish();
     }
     if (tid == 0) {
-        mbar_init(&bar_tma, 1);
+        mbar_init(&bar_tma[0], 1);
+        mbar_init(&bar_tma[1], 1);
         mbar_init(&bar_mma, 1);
         fence_mbar_init();
         s_abort = 0;
     }
-    fence_proxy_async();  // the weights written above are read by the tensor cores
-    tc_before_sync();
-    __syncthreads();
-    tc_after_sync();
-    const uint32_t tmem = tmem_base;
-    uint32_t ph_tma = 0, ph_mma = 0;
-    for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x) {
+    __syncthreads();  // seg_off and the barriers are ready
+    // tile base index: tile number with zeros inserted at the tile qubits
+    auto tile_base = [&](uint64_t t) {
         uint64_t base = t;
         for (uint32_t p = 0; p < k; ++p) {
             const uint32_t q = P.tq[p];
             base = ((base >> q) << (q + 1)) | (base & ((1ull << q) - 1ull));
         }
-        if (warp == 0) {
-            if (lane == 0) {
-                fence_proxy_async();
-                mbar_expect_tx(&bar_tma, (1u << k) * 8u);
-            }
-            __syncwarp();
-            for (uint32_t s = lane; s < nseg; s += 32)
-                bulk_load(tile + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 8u, &bar_tma);
+        return base;
+    };
+    // warp 0 issues the bulk copies of one tile into buffer `buf`
+    auto load_tile = [&](uint64_t t, uint32_t buf) {
+        const uint64_t base = tile_base(t);
+        float2* tile = tiles + (size_t)buf * 4096;
+        if (lane == 0) {
+            fence_proxy_async();
+            mbar_expect_tx(&bar_tma[buf], (1u << k) * 8u);
         }
-        if (!mbar_wait(&bar_tma, ph_tma)) {
+        __syncwarp();
+        for (uint32_t s = lane; s < nseg; s += 32)
+            bulk_load(tile + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 8u, &bar_tma[buf]);
+    };
+    if (warp == 0 && (uint64_t)blockIdx.x < P.ntiles) load_tile(blockIdx.x, 0);
+    fence_proxy_async();  // the weights written above are read by the tensor cores
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = tmem_base;
+    uint32_t ph_tma[2] = {0, 0};
+    uint32_t ph_mma = 0;
+    uint32_t it = 0;
+    for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x, ++it) {
+        const uint32_t cur = it & 1u;
+        float2* tile = tiles + (size_t)cur * 4096;
+        if (!mbar_wait(&bar_tma[cur], ph_tma[cur])) {
             atomicExch(err, 1);
             s_abort = 1;
         }
-        ph_tma ^= 1u;
+        ph_tma[cur] ^= 1u;
         __syncthreads();
         if (s_abort) break;
+        if (warp == 0 && t + gridDim.x < P.ntiles) {
+            bulk_wait_read();  // the store of the other buffer has read it
+            load_tile(t + gridDim.x, cur ^ 1u);
+        }
         for (uint32_t b = 0; b < nb; ++b) {
-            // A[m][2r + c] = component c of the tile amplitude (m, r), split into TF32 hi and lo
+            // A[m][2r + c] = component c of the tile amplitude (m, r), split into TF32 hi and lo;
+            // a warp covers 8 rows x 4 amplitudes, so its 64-bit stores take two wavefronts
             for (uint32_t i = tid; i < 4096u; i += kNT) {
-                const uint32_t m = i & 127u, r = i >> 7;
+                const uint32_t m = (i & 7u) | (((i >> 5) & 15u) << 3);
+                const uint32_t r = ((i >> 3) & 3u) | (((i >> 9) & 7u) << 2);
                 const float2 x = tile[mpos[b][m] + rpos[b][r]];
                 const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
                 const uint32_t o = op_off(m, 2 * r);
@@ -305,16 +327,16 @@ __global__ void __launch_bounds__(kNT, 1)
         fence_proxy_async();
         __syncthreads();
         if (warp == 0) {
+            const uint64_t base = tile_base(t);
             for (uint32_t s = lane; s < nseg; s += 32)
                 bulk_store(psi + (base | seg_off[s]), tile + (size_t)s * seg_amps, seg_amps * 8u);
             bulk_commit();
-            bulk_wait_read();
         }
-        __syncthreads();
     }
     if (s_abort) {
-        // copies or MMAs may still be in flight: wait for both barriers once more (bounded)
-        mbar_wait(&bar_tma, ph_tma);
+        // copies or MMAs may still be in flight: wait on every barrier once more (bounded)
+        mbar_wait(&bar_tma[0], ph_tma[0]);
+        mbar_wait(&bar_tma[1], ph_tma[1]);
         mbar_wait(&bar_mma, ph_mma);
     }
     if (warp == 0) bulk_wait_all();
@@ -573,7 +595,7 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     TRY_LAUNCH(launch_norm_sqr_sum(r->psi, r->fmt, r->len, r->scratch, d_norm0, r->stream));
     static const bool attr = [] {
         return cudaFuncSetAttribute((const void*)precision_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(kSmemTile + 2 * kSmemA + kMaxPB * kSmemW)) == cudaSuccess;
+                                    (int)(2 * kSmemTile + 2 * kSmemA + kMaxPB * kSmemW)) == cudaSuccess;
     }();
     if (!attr) return set_error(QVNT_ERR_CUDA, "precision kernel: shared-memory attribute refused");
     int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
@@ -601,7 +623,7 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
                 if ((b.sup >> q) & 1ull) P.blocks[j].bits[jj++] = (uint8_t)pos_of[q];
             P.blocks[j].w_off = (uint32_t)(p.members[j] * 2 * kWFloats);
         }
-        const size_t smem = kSmemTile + 2 * kSmemA + P.nblocks * kSmemW;
+        const size_t smem = 2 * kSmemTile + 2 * kSmemA + P.nblocks * kSmemW;
         uint64_t grid = (uint64_t)r->ctx->geo.sms;
         if (grid > P.ntiles) grid = P.ntiles;
         cudaEvent_t stop = nullptr;

@@ -115,7 +115,7 @@ def test_batch_autotune_and_errors():
     w = _workload(16, 71, (8, 14), (2, 4), measure=True)
     b = Batch(w.q_nums, w.states, w.gates, w.offsets, w.masks)
     k, budget, ms = b.autotune(stride=2)
-    assert k in (11, 12) and budget in (100, 200, 400, 800) and ms > 0
+    assert k in (11, 12) and budget in (200, 400, 800, 1600) and ms > 0
     assert b.info()["fusion_k"] == k
     with pytest.raises(QvntError):
         b.run()  # measuring batches need draws
