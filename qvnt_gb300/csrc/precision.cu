@@ -42,7 +42,7 @@ namespace {
 constexpr int kPT = 12;            // tile qubits
 constexpr int kBQ = 5;             // block qubits
 constexpr int kBD = 1 << kBQ;      // block dimension
-constexpr int kNT = 256;           // threads: 8 warps, two per tensor-memory lane quadrant
+constexpr int kNT = 512;           // threads: 16 warps, four per tensor-memory lane quadrant
 constexpr int kMaxPB = 2;          // blocks per pass (their weights stay in shared memory)
 constexpr int kRenormEvery = 10;   // passes between FP64 norm restorations
 constexpr uint32_t kPWaitLimit = 1u << 22;
@@ -148,15 +148,13 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
                  : "memory");
 }
-// 32 consecutive accumulator columns of this thread's lane.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+// 16 consecutive accumulator columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
         : "r"(taddr)
         : "memory");
 }
@@ -274,16 +272,22 @@ __global__ void __launch_bounds__(kNT, 1)
             load_tile(t + gridDim.x, cur ^ 1u);
         }
         for (uint32_t b = 0; b < nb; ++b) {
-            // A[m][2r + c] = component c of the tile amplitude (m, r), split into TF32 hi and lo;
-            // a warp covers 8 rows x 4 amplitudes, so its 64-bit stores take two wavefronts
-            for (uint32_t i = tid; i < 4096u; i += kNT) {
-                const uint32_t m = (i & 7u) | (((i >> 5) & 15u) << 3);
-                const uint32_t r = ((i >> 3) & 3u) | (((i >> 9) & 7u) << 2);
-                const float2 x = tile[mpos[b][m] + rpos[b][r]];
-                const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
-                const uint32_t o = op_off(m, 2 * r);
-                *reinterpret_cast<float2*>(a_hi + o) = make_float2(hr, hm);
-                *reinterpret_cast<float2*>(a_lo + o) = make_float2(x.x - hr, x.y - hm);
+            // A[m][2r + c] = component c of the tile amplitude (m, r), split into TF32 hi and lo.
+            // Element i = tid + 512 j: row m = tid bits 0-2 and 5-8 (fixed per thread), amplitude
+            // r = tid bits 3-4 | j << 2, so both addresses are a per-thread base plus a per-j
+            // constant; a warp covers 8 rows x 4 amplitudes (64-bit stores in two wavefronts).
+            {
+                const uint32_t m = (tid & 7u) | ((tid >> 5) << 3);
+                const uint32_t rlo = (tid >> 3) & 3u;
+                const uint32_t tb = mpos[b][m] + rpos[b][rlo];
+                const uint32_t ab = op_off(m, 2 * rlo);
+#pragma unroll
+                for (uint32_t j = 0; j < 8; ++j) {
+                    const float2 x = tile[tb + rpos[b][4 * j]];
+                    const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
+                    *reinterpret_cast<float2*>(a_hi + ab + 64 * j) = make_float2(hr, hm);
+                    *reinterpret_cast<float2*>(a_lo + ab + 64 * j) = make_float2(x.x - hr, x.y - hm);
+                }
             }
             fence_proxy_async();
             tc_before_sync();
@@ -309,16 +313,16 @@ __global__ void __launch_bounds__(kNT, 1)
             }
             ph_mma ^= 1u;
             tc_after_sync();
-            // warp w: accumulator lanes 32 (w % 4) .. + 31 (rows m), columns 32 (w / 4) .. + 31
-            uint32_t v[32];
-            tmem_ld32(tmem + ((32u * (warp & 3u)) << 16) + 32u * (warp >> 2), v);
+            // warp w: accumulator lanes 32 (w % 4) .. + 31 (rows m), columns 16 (w / 4) .. + 15
+            uint32_t v[16];
+            tmem_ld16(tmem + ((32u * (warp & 3u)) << 16) + 16u * (warp >> 2), v);
             tmem_ld_wait();
             const uint32_t m = 32u * (warp & 3u) + lane;
             const uint32_t mp = mpos[b][m];
 #pragma unroll
-            for (uint32_t j = 0; j < 16; ++j)
-                tile[mp + rpos[b][16u * (warp >> 2) + j]] = make_float2(__uint_as_float(v[2 * j]),
-                                                                        __uint_as_float(v[2 * j + 1]));
+            for (uint32_t j = 0; j < 8; ++j)
+                tile[mp + rpos[b][8u * (warp >> 2) + j]] = make_float2(__uint_as_float(v[2 * j]),
+                                                                       __uint_as_float(v[2 * j + 1]));
             tc_before_sync();
             __syncthreads();
             if (s_abort) break;
