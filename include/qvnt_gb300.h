@@ -335,7 +335,7 @@ int qvnt_batch_info(const qvnt_batch* batch, uint64_t* items, uint64_t* passes, 
  *                        for a request that keeps its amplitudes).  Among the queued requests that
  *                        fit, the one with the least work (amplitudes x gates) discounted by
  *                        exp(-waiting seconds) goes next; requests of 24 qubits or more hold at most
- *                        a quarter of the slots.  Requests beyond `max_queue` queued ones are shed
+ *                        a quarter of the slots (at most 8).  Requests beyond `max_queue` queued ones are shed
  *                        (QVNT_ERR_BUSY; 0 = 4096).
  *   qvnt_server_submit   copies the request (gates validated against the register); `arrival_s` is
  *                        its arrival on the server clock (qvnt_server_clock; < 0 = now), the start of

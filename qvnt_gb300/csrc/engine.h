@@ -54,6 +54,7 @@ struct qvnt_reg {
     uint64_t passes = 0;
     uint64_t last_measured_index = 0;
     bool timing = false;
+    bool tile_grid = false;  // one CTA per tile instead of a persistent grid (shared-GPU serving)
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
     qvnt::FusedState fused;
 };

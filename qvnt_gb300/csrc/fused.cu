@@ -1481,7 +1481,9 @@ int launch_passes(qvnt_reg* r, const qvnt_gate* gates, const std::vector<EGate>&
         std::copy(enc.stages.begin(), enc.stages.end(), P->stages);
         std::copy(enc.gates.begin(), enc.gates.end(), P->gates);
         std::copy(enc.coef.begin(), enc.coef.end(), P->coef);
-        uint64_t grid = (uint64_t)r->ctx->geo.sms * per_sm;
+        // persistent grid by default; one CTA per tile when the register shares the GPU with others
+        // (CTAs then retire every tile, so other streams' higher-priority work gets SMs quickly)
+        uint64_t grid = r->tile_grid ? P->ntiles : (uint64_t)r->ctx->geo.sms * per_sm;
         if (grid > P->ntiles) grid = P->ntiles;
         cudaEvent_t stop = nullptr;
         status = timing_begin(r, &stop);

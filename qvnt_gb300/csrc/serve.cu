@@ -13,7 +13,8 @@
 // Registers are pooled by size and reused through `qvnt_reg_reset`, so steady-state admission
 // allocates nothing and never hits the device-wide synchronisation of cudaFree; idle pooled
 // registers are freed only when a new size needs their memory.  Streams of small registers get the
-// higher stream priority, so their blocks overtake the long passes of large ones.
+// higher stream priority, and every server register launches one CTA per tile (not a persistent
+// grid), so the blocks of small requests overtake the long passes of large ones at tile granularity.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -35,8 +36,8 @@ using Clock = std::chrono::steady_clock;
 
 constexpr uint32_t kMagicServer = 0x51535256u;
 constexpr double kAgeScale = 1.0;  // seconds: waiting time that discounts a request's work by e
-// Requests whose state is at least kLargeBytes are "large": at most a quarter of the slots run
-// them at once, so that long requests cannot hold every slot while short ones queue.
+// Requests whose state is at least kLargeBytes are "large": at most a quarter of the slots (and at
+// most 8) run them at once, so that long requests cannot hold every slot while short ones queue.
 constexpr uint64_t kLargeBytes = 16ull << 24;  // a 24-qubit state
 
 struct Request {
@@ -108,7 +109,7 @@ int priority_for(const qvnt_server* s, uint32_t n) {
 // after waiting about kAgeScale * ln(work ratio).  Returns queue.end() when none fits.
 std::deque<Request*>::iterator pick(qvnt_server* s) {
     const double t = s->now();
-    const uint64_t max_large = std::max<uint64_t>(1, s->slots / 4);
+    const uint64_t max_large = std::max<uint64_t>(1, std::min<uint64_t>(8, s->slots / 4));
     auto best = s->queue.end();
     double best_score = 0.0;
     for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
@@ -189,6 +190,7 @@ void worker(qvnt_server* s) {
         } else {
             st = qvnt_reg_create(s->ctx, r->n, r->state, &reg);
             if (!st) st = qvnt::reg_set_priority(reg, priority_for(s, r->n));
+            if (!st) reg->tile_grid = true;
         }
         if (!st) st = run_request(s, r, reg);
         std::string err = st ? qvnt_last_error() : std::string();
