@@ -1285,13 +1285,16 @@ struct PlannedPass {
     std::vector<size_t> members;  // indices into the engine gate list
 };
 
-// Pass budget in estimated FP32 instructions per amplitude (form_cost units): about what one HBM
-// round trip of the tile hides (32 B per amplitude at ~6.8 TB/s against ~114 FFMA/clk/SM).
+// Pass budget in estimated FP32 instructions per amplitude (form_cost units).  One HBM round trip
+// of a tile hides about 200 (32 B per amplitude at ~6.8 TB/s against ~114 FFMA/clk/SM), but on GB300
+// double-float passes are compute-bound, so fewer, heavier passes win: measured on the 30-qubit
+// random circuit, 200 -> 330 passes, 505 gate-passes/s; 450 -> 151, 532; 800 -> 130, 539;
+// 1400 -> 121, 540.
 int pass_budget() {
     static int b = [] {
         const char* e = std::getenv("QVNT_PASS_BUDGET");
         const int v = e ? std::atoi(e) : 0;
-        return v > 0 ? v : 200;
+        return v > 0 ? v : 800;
     }();
     return b;
 }
