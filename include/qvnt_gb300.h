@@ -265,6 +265,18 @@ int qvnt_norm_sqr_noalloc(const double* d_psi, uint64_t len, double* d_out, void
  * Counters for measurement: kernels launched and fused passes run by this register so far.
  * ------------------------------------------------------------------------------------------- */
 int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* passes);
+/* `Reg::sample_all(count)` (src/register/quant.rs:513-594): a histogram of `count` measurements
+ * without collapse, p_i count plus Gaussian noise, corrected to sum to `count`.  out_counts gets 2^n
+ * entries.  `normals` (2^n standard normal draws, host memory) replaces qvnt's thread_rng draws when
+ * given; otherwise the draws come from `seed` on the device.  Registers below 3 qubits are rejected
+ * (qvnt panics there: its probability vector is shorter than the padded buffer it walks). */
+int qvnt_reg_sample_all(qvnt_reg* reg, uint64_t count, uint64_t seed, const double* normals, uint64_t* out_counts);
+/* `Reg::combine_with_unitary((a, b), c)` (quant.rs:273-308): a new register of n + 1 qubits whose lower
+ * half is c00 a + c01 b and upper half c10 a + c11 b; c is a unitary 2x2 complex matrix, interleaved. */
+int qvnt_reg_combine_with_unitary(const qvnt_reg* a, const qvnt_reg* b, const double* c, qvnt_reg** out);
+/* `Reg::linear_composition(psi, (c0, c1))` (quant.rs:311-328): self = self * c0 + psi * c1; c holds
+ * c0 and c1 interleaved (re, im). */
+int qvnt_reg_linear_composition(qvnt_reg* self, const qvnt_reg* psi, const double* c);
 /* State comparison in FP64 across engines (no counterpart in the reference): fidelity
  * |<a|b>|^2 / (<a|a> <b|b>) and max_i |a_i - b_i|.  Registers of the same size and context. */
 int qvnt_reg_overlap(const qvnt_reg* a, const qvnt_reg* b, double* fidelity, double* max_abs_diff);

@@ -350,6 +350,70 @@ void oracle_tensor(const oc_t* a, uint32_t na, const oc_t* b, uint32_t nb, oc_t*
     }
 }
 
+/* src/register/quant.rs:513-594.  p = get_probabilities(); n_i = sqrt(p_i) * z_i; n_sum = the
+ * sequential sum; counts (p_i c + sqrt(c) (n_i - n_sum p_i)).round().max(0); then the total is
+ * corrected to `count`: a deficit adds (delta >> q_num) to every entry and one more to the first
+ * (delta % q_mask) entries (q_mask, not q_size, as written there); an excess removes one at a time
+ * from the first nonzero entries of idx & q_mask, idx = 0, 1, ... */
+int oracle_sample_all(const oc_t* psi, uint64_t len, uint32_t q_num, uint64_t count, const double* z,
+                      uint64_t* out) {
+    const uint64_t q_size = 1ull << q_num, q_mask = q_size - 1;
+    if (len != q_size || q_mask == 0) return -1;
+    double* p = (double*)malloc(q_size * sizeof(double));
+    double* n = (double*)malloc(q_size * sizeof(double));
+    oracle_get_probabilities(psi, len, q_num, p);
+    const double c = (double)count;
+    const double c_sqrt = sqrt(c);
+    for (uint64_t i = 0; i < q_size; ++i) n[i] = sqrt(p[i]) * z[i];
+    double n_sum = 0.0;
+    for (uint64_t i = 0; i < q_size; ++i) n_sum += n[i];
+    int64_t total = 0;
+    for (uint64_t i = 0; i < q_size; ++i) {
+        double v = round(c * p[i] + c_sqrt * (n[i] - n_sum * p[i]));
+        int64_t k = v != v ? 0 : (int64_t)v;  /* Rust `as` maps NaN to 0 */
+        out[i] = (uint64_t)(k > 0 ? k : 0);
+        total += (int64_t)out[i];
+    }
+    int64_t delta = total - (int64_t)count;
+    if (delta < 0) {
+        const uint64_t d = (uint64_t)(-delta);
+        const uint64_t d0 = d >> q_num, d1 = d % q_mask;
+        for (uint64_t idx = 0; idx < len; ++idx) {
+            out[idx] += d0;
+            if (idx < d1) out[idx] += 1;
+        }
+    } else if (delta > 0) {
+        uint64_t d = (uint64_t)delta;
+        for (uint64_t idx = 0; d != 0; ++idx) {
+            if (out[idx & q_mask] == 0) continue;
+            out[idx & q_mask] -= 1;
+            d -= 1;
+        }
+    }
+    free(p);
+    free(n);
+    return 0;
+}
+
+/* src/register/quant.rs:273-308: idx with no bit above q_mask takes c00 a + c01 b, the others
+ * c10 a + c11 b, where a = a[idx & q_mask], b = b[idx & q_mask] (num-complex Mul and Add). */
+void oracle_combine_with_unitary(const oc_t* a, const oc_t* b, uint32_t n, const double* c, oc_t* out) {
+    const uint64_t q_mask = (1ull << n) - 1;
+    const uint64_t len = oracle_reg_len(n + 1);
+    const oc_t c00 = {c[0], c[1]}, c01 = {c[2], c[3]}, c10 = {c[4], c[5]}, c11 = {c[6], c[7]};
+    for (uint64_t idx = 0; idx < len; ++idx) {
+        const oc_t qa = a[q_mask & idx], qb = b[q_mask & idx];
+        if ((~q_mask & idx) == 0) out[idx] = c_add(c_mul(c00, qa), c_mul(c01, qb));
+        else out[idx] = c_add(c_mul(c10, qa), c_mul(c11, qb));
+    }
+}
+
+/* src/register/quant.rs:311-328: q.0 = q.0 * c.0 + q.1 * c.1. */
+void oracle_linear_composition(oc_t* self, const oc_t* psi, uint64_t len, const double* c) {
+    const oc_t c0 = {c[0], c[1]}, c1 = {c[2], c[3]};
+    for (uint64_t i = 0; i < len; ++i) self[i] = c_add(c_mul(self[i], c0), c_mul(psi[i], c1));
+}
+
 /* ---- builders (src/operator/...) ---------------------------------------------------------- */
 /* float-cmp 0.8 `approx_eq!(f64, x, y, ulps = 2)`: equal, within f64::EPSILON, or within 2 ULPs
  * (src/math/approx_cmp.rs:5-10). */

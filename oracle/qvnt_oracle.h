@@ -56,6 +56,16 @@ void oracle_reset_by_mask(oc_t* psi, uint64_t len, uint32_t q_num, uint64_t mask
 void oracle_get_polar(const oc_t* psi, uint32_t q_num, double* out);              /* :417-431 */
 /* Tensor product (quant.rs:330-371); out has oracle_reg_len(na + nb) amplitudes. */
 void oracle_tensor(const oc_t* a, uint32_t na, const oc_t* b, uint32_t nb, oc_t* out);
+/* `Reg::sample_all(count)` (quant.rs:513-594) with the standard-normal draws injected: z[i], i < 2^n.
+ * out gets 2^n counts.  Returns -1 where qvnt panics (n < 3: its probability vector is shorter than
+ * the padded buffer it indexes), else 0. */
+int oracle_sample_all(const oc_t* psi, uint64_t len, uint32_t q_num, uint64_t count, const double* z,
+                      uint64_t* out);
+/* `Reg::combine_with_unitary((a, b), c)` (quant.rs:273-308) for two registers of n qubits: out has
+ * oracle_reg_len(n + 1) amplitudes; c is a 2x2 complex matrix, interleaved (re, im). */
+void oracle_combine_with_unitary(const oc_t* a, const oc_t* b, uint32_t n, const double* c, oc_t* out);
+/* `Reg::linear_composition(psi, (c0, c1))` (quant.rs:311-328): self = self * c0 + psi * c1. */
+void oracle_linear_composition(oc_t* self, const oc_t* psi, uint64_t len, const double* c);
 
 /* Builders (src/operator/...).  List builders return the number of gates; out may be NULL. */
 int oracle_gate_make(uint32_t kind, uint64_t a_mask, uint64_t b_mask, double angle,

@@ -86,6 +86,9 @@ _PROTOS = {
     "qvnt_reg_create": (c_int, [c_void, c_u32, c_u64, P(c_void)]),
     "qvnt_reg_create_ex": (c_int, [c_void, c_u32, c_u64, c_int, P(c_void)]),
     "qvnt_reg_overlap": (c_int, [c_void, c_void, P(c_double), P(c_double)]),
+    "qvnt_reg_sample_all": (c_int, [c_void, c_u64, c_u64, c_void, c_void]),
+    "qvnt_reg_combine_with_unitary": (c_int, [c_void, c_void, P(c_double), P(c_void)]),
+    "qvnt_reg_linear_composition": (c_int, [c_void, c_void, P(c_double)]),
     "qvnt_precision_plan_info": (c_int, [P(QvntGate), c_size, c_u32, P(c_u64), P(c_u64)]),
     "qvnt_reg_destroy": (c_int, [c_void]),
     "qvnt_reg_clone": (c_int, [c_void, P(c_void)]),

@@ -728,6 +728,105 @@ int qvnt_reg_get_stream(const qvnt_reg* reg, void** stream) {
     return QVNT_OK;
 }
 
+int qvnt_reg_sample_all(qvnt_reg* reg, uint64_t count, uint64_t seed, const double* normals, uint64_t* out_counts) {
+    CHECK_REG(reg);
+    if (!out_counts) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
+    const uint64_t q_size = 1ull << reg->q_num;
+    if (reg->len != q_size || q_size < 2)  // quant.rs:515-538 indexes p (2^n entries) over psi.len()
+        return set_error(QVNT_ERR_BAD_ARG, "sample_all needs at least 3 qubits (qvnt panics below)");
+    QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
+    const uint64_t nc = chunk_count(q_size);
+    double* d_abs = reg->scratch + 2 * nc;
+    double* d_inv = d_abs + 1;
+    double* d_nsum = d_abs + 2;
+    int* d_status = reinterpret_cast<int*>(reinterpret_cast<char*>(reg->d_small) + 8);
+    double* d_n = nullptr;
+    double* d_z = nullptr;
+    cudaError_t e = cudaMalloc(&d_n, q_size * sizeof(double));
+    if (e == cudaSuccess && normals) e = cudaMalloc(&d_z, q_size * sizeof(double));
+    if (e == cudaSuccess && normals)
+        e = cudaMemcpyAsync(d_z, normals, q_size * sizeof(double), cudaMemcpyHostToDevice, reg->stream);
+    int st = QVNT_OK;
+    std::vector<long long> h(q_size);
+    if (e == cudaSuccess) {
+        st = launch_norm_sqr_sum(reg->psi, reg->fmt, reg->len, reg->scratch, d_abs, reg->stream);
+        if (!st) st = launch_inv(d_abs, d_inv, d_status, reg->stream);
+        if (!st) st = launch_sample_all(reg->psi, reg->fmt, q_size, d_inv, d_z, seed, count, d_n, reg->scratch, d_nsum,
+                                        reg->stream);
+        if (!st) e = cudaMemcpyAsync(h.data(), d_n, q_size * sizeof(long long), cudaMemcpyDeviceToHost, reg->stream);
+        if (!st && e == cudaSuccess) e = cudaStreamSynchronize(reg->stream);
+        reg->launches += 6;
+    }
+    if (d_n) cudaFree(d_n);
+    if (d_z) cudaFree(d_z);
+    if (st) return st;
+    if (e != cudaSuccess) return set_cuda_error(e, "sample_all");
+    // correction of the total to `count` (quant.rs:562-591), sequential as there
+    const uint64_t q_mask = q_size - 1;
+    long long total = 0;
+    for (uint64_t i = 0; i < q_size; ++i) {
+        out_counts[i] = (uint64_t)h[i];
+        total += h[i];
+    }
+    const long long delta = total - (long long)count;
+    if (delta < 0) {
+        const uint64_t d = (uint64_t)(-delta);
+        const uint64_t d0 = d >> reg->q_num, d1 = d % q_mask;
+        for (uint64_t idx = 0; idx < q_size; ++idx) out_counts[idx] += d0 + (idx < d1 ? 1 : 0);
+    } else if (delta > 0) {
+        uint64_t d = (uint64_t)delta;
+        for (uint64_t idx = 0; d != 0; ++idx) {
+            if (out_counts[idx & q_mask] == 0) continue;
+            out_counts[idx & q_mask] -= 1;
+            d -= 1;
+        }
+    }
+    return QVNT_OK;
+}
+
+int qvnt_reg_combine_with_unitary(const qvnt_reg* a, const qvnt_reg* b, const double* c, qvnt_reg** out) {
+    CHECK_REG(a);
+    CHECK_REG(b);
+    if (!c || !out) return set_error(QVNT_ERR_BAD_ARG, "null argument");
+    if (a->ctx != b->ctx) return set_error(QVNT_ERR_BAD_ARG, "registers belong to different contexts");
+    if (a->q_num != b->q_num)  // quant.rs:277: None
+        return set_error(QVNT_ERR_BAD_ARG, "registers of %u and %u qubits", a->q_num, b->q_num);
+    if (a->fmt == FMT_C32 || b->fmt == FMT_C32)
+        return set_error(QVNT_ERR_UNSUPPORTED, "combine of precision-engine registers");
+    if (a->q_num + 1 > kMaxQubits) return set_error(QVNT_ERR_BAD_ARG, "result too large");
+    qvnt_gate chk;
+    TRY(qvnt_gate_make(QVNT_GATE_U1, 1, 0, 0.0, c, &chk));  // quant.rs:275: is_unitary_m1
+    QVNT_CUDA_TRY(cudaSetDevice(a->ctx->device));
+    QVNT_CUDA_TRY(cudaStreamSynchronize(a->stream));
+    QVNT_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    qvnt_reg* r = nullptr;
+    TRY(make_reg(a->ctx, a->q_num + 1, a->engine, &r));
+    int st = launch_combine(a->psi, a->fmt, b->psi, b->fmt, a->q_num, c, r->psi, r->fmt, r->len, r->stream);
+    if (st) {
+        reg_free(r);
+        return st;
+    }
+    r->launches += 1;
+    *out = r;
+    return QVNT_OK;
+}
+
+int qvnt_reg_linear_composition(qvnt_reg* self, const qvnt_reg* psi, const double* c) {
+    CHECK_REG(self);
+    CHECK_REG(psi);
+    if (!c) return set_error(QVNT_ERR_BAD_ARG, "null coefficients");
+    if (self->len != psi->len)  // quant.rs:312: assert_eq!
+        return set_error(QVNT_ERR_BAD_ARG, "buffers of %llu and %llu amplitudes", (unsigned long long)self->len,
+                         (unsigned long long)psi->len);
+    if (self->fmt == FMT_C32 || psi->fmt == FMT_C32)
+        return set_error(QVNT_ERR_UNSUPPORTED, "linear composition of precision-engine registers");
+    QVNT_CUDA_TRY(cudaSetDevice(self->ctx->device));
+    QVNT_CUDA_TRY(cudaStreamSynchronize(psi->stream));
+    TRY(launch_linear(self->psi, self->fmt, psi->psi, psi->fmt, self->len, c, self->stream));
+    self->launches += 1;
+    return QVNT_OK;
+}
+
 int qvnt_reg_overlap(const qvnt_reg* a, const qvnt_reg* b, double* fidelity, double* max_abs_diff) {
     CHECK_REG(a);
     CHECK_REG(b);

@@ -57,6 +57,18 @@ int launch_convert_fmt(const double2* src, int fsrc, double2* dst, int fdst, uin
 // psi *= sqrt(*d_target / *d_current) (restores a norm after rounding drift; nothing when either is 0).
 int launch_rescale(double2* psi, int fmt, uint64_t len, const double* d_target, const double* d_current,
                    cudaStream_t stream);
+// sample_all's device part: d_n[i] (q_size doubles) ends as the int64 counts before the host's
+// total correction; d_z: injected standard normals (q_size) or null for seeded draws;
+// scratch: chunk_count(q_size) doubles; *d_nsum gets the sum of the noise terms.
+int launch_sample_all(const double2* psi, int fmt, uint64_t q_size, const double* d_inv, const double* d_z,
+                      uint64_t seed, uint64_t count, double* d_n, double* scratch, double* d_nsum,
+                      cudaStream_t stream);
+// combine_with_unitary: out (out_len) from a, b of n qubits and the 2x2 complex c (interleaved).
+int launch_combine(const double2* a, int fa, const double2* b, int fb, uint32_t n, const double* c, double2* out,
+                   int fo, uint64_t out_len, cudaStream_t stream);
+// linear_composition: self = self * c[0] + psi * c[1] (c: two complex numbers, interleaved).
+int launch_linear(double2* self, int fs, const double2* psi, int fp, uint64_t len, const double* c,
+                  cudaStream_t stream);
 // <a|b> (re, im), <a|a>, <b|b> and max_i |a_i - b_i| into d_out[0..4]; scratch: 5 * chunk_count(len).
 int launch_overlap(const double2* a, int fa, const double2* b, int fb, uint64_t len, double* scratch, double* d_out,
                    cudaStream_t stream);

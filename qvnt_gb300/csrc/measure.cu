@@ -356,6 +356,80 @@ __global__ void __launch_bounds__(kScanThreads) overlap_final_kernel(const doubl
     }
 }
 
+// Standard normal draw for sample_all when the caller injects none: two uniforms from SplitMix64 of
+// (seed, index), Box-Muller with the device's log / sqrt / cospi.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double std_normal(uint64_t seed, uint64_t i) {
+    const uint64_t a = mix64(seed ^ (2 * i)), b = mix64(seed ^ (2 * i + 1));
+    const double u1 = ((double)(a >> 11) + 1.0) * (1.0 / 9007199254740992.0);  // (0, 1]
+    const double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);          // [0, 1)
+    return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+// sample_all, step 1 (quant.rs:513-535): n_i = sqrt(p_i) z_i with p_i = |psi_i|^2 * inv, into n[];
+// chunk partial sums of n for n_sum.
+template <class Acc>
+__global__ void __launch_bounds__(kRedThreads) sample_noise_kernel(const double2* __restrict__ psi, uint64_t q_size,
+                                                                    const double* __restrict__ d_inv,
+                                                                    const double* __restrict__ z, uint64_t seed,
+                                                                    double* __restrict__ n, double* __restrict__ part) {
+    __shared__ double sm[32];
+    const double inv = *d_inv;
+    const uint64_t base = (uint64_t)blockIdx.x * kChunk;
+    double s = 0.0;
+    for (uint32_t k = threadIdx.x; k < kChunk; k += kRedThreads) {
+        const uint64_t i = base + k;
+        if (i >= q_size) break;
+        const double p = nsq(Acc::load(psi, i)) * inv;
+        const double v = sqrt(p) * (z ? z[i] : std_normal(seed, i));
+        n[i] = v;
+        s += v;
+    }
+    const double t = block_sum<kRedThreads>(s, sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// sample_all, step 2 (quant.rs:537-543): counts (c p_i + sqrt(c) (n_i - n_sum p_i)).round().max(0),
+// written over n[] as int64.
+template <class Acc>
+__global__ void sample_count_kernel(const double2* __restrict__ psi, uint64_t q_size, const double* __restrict__ d_inv,
+                                    const double* __restrict__ d_nsum, double c, double* __restrict__ n) {
+    const double inv = *d_inv, n_sum = *d_nsum, c_sqrt = sqrt(c);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < q_size; i += stride) {
+        const double p = nsq(Acc::load(psi, i)) * inv;
+        const double v = round(c * p + c_sqrt * (n[i] - n_sum * p));
+        const long long k = isnan(v) ? 0 : (long long)v;
+        reinterpret_cast<long long*>(n)[i] = k > 0 ? k : 0;
+    }
+}
+
+// combine_with_unitary (quant.rs:273-308) and linear_composition (quant.rs:311-328).
+template <class AccA, class AccB, class AccO>
+__global__ void combine_kernel(const double2* __restrict__ a, const double2* __restrict__ b, uint64_t q_mask,
+                               double2 c00, double2 c01, double2 c10, double2 c11, double2* __restrict__ out,
+                               uint64_t out_len) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < out_len; i += stride) {
+        const double2 qa = AccA::load(a, q_mask & i), qb = AccB::load(b, q_mask & i);
+        const bool low = (~q_mask & i) == 0;
+        AccO::store(out, i, low ? c_add(c_mul(c00, qa), c_mul(c01, qb)) : c_add(c_mul(c10, qa), c_mul(c11, qb)));
+    }
+}
+
+template <class Acc, class AccP>
+__global__ void linear_kernel(double2* __restrict__ self, const double2* __restrict__ psi, uint64_t len, double2 c0,
+                              double2 c1) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        Acc::store(self, i, c_add(c_mul(Acc::load(self, i), c0), c_mul(AccP::load(psi, i), c1)));
+}
+
 // Storage conversion in place: f64 -> df64 (to_df = 1) or df64 -> f64 (to_df = 0).
 __global__ void convert_kernel(double2* __restrict__ psi, uint64_t len, int to_df) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -506,6 +580,56 @@ void overlap_with(const double2* a, const double2* b, int fb, uint64_t len, doub
     else overlap_chunk_kernel<AccA, AccF64><<<nc, kRedThreads, 0, stream>>>(a, b, len, part);
 }
 }  // namespace
+
+int launch_sample_all(const double2* psi, int fmt, uint64_t q_size, const double* d_inv, const double* d_z,
+                      uint64_t seed, uint64_t count, double* d_n, double* scratch, double* d_nsum,
+                      cudaStream_t stream) {
+    const uint64_t nc = chunk_count(q_size);
+    QVNT_BY_FMT(fmt, sample_noise_kernel,
+                <<<(unsigned)nc, kRedThreads, 0, stream>>>(psi, q_size, d_inv, d_z, seed, d_n, scratch));
+    final_sum_kernel<<<1, kScanThreads, 0, stream>>>(scratch, nc, d_nsum);
+    QVNT_BY_FMT(fmt, sample_count_kernel,
+                <<<flat_grid(q_size), 256, 0, stream>>>(psi, q_size, d_inv, d_nsum, (double)count, d_n));
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_combine(const double2* a, int fa, const double2* b, int fb, uint32_t n, const double* c, double2* out,
+                   int fo, uint64_t out_len, cudaStream_t stream) {
+    const uint64_t q_mask = (1ull << n) - 1;
+    const double2 c00 = make_double2(c[0], c[1]), c01 = make_double2(c[2], c[3]);
+    const double2 c10 = make_double2(c[4], c[5]), c11 = make_double2(c[6], c[7]);
+    const unsigned g = flat_grid(out_len);
+    const int code = (fa << 2) | (fb << 1) | fo;
+#define QVNT_COMBINE(A, B, O) combine_kernel<A, B, O><<<g, 256, 0, stream>>>(a, b, q_mask, c00, c01, c10, c11, out, out_len)
+    switch (code) {
+    case 0: QVNT_COMBINE(AccF64, AccF64, AccF64); break;
+    case 1: QVNT_COMBINE(AccF64, AccF64, AccDF64); break;
+    case 2: QVNT_COMBINE(AccF64, AccDF64, AccF64); break;
+    case 3: QVNT_COMBINE(AccF64, AccDF64, AccDF64); break;
+    case 4: QVNT_COMBINE(AccDF64, AccF64, AccF64); break;
+    case 5: QVNT_COMBINE(AccDF64, AccF64, AccDF64); break;
+    case 6: QVNT_COMBINE(AccDF64, AccDF64, AccF64); break;
+    default: QVNT_COMBINE(AccDF64, AccDF64, AccDF64); break;
+    }
+#undef QVNT_COMBINE
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
+
+int launch_linear(double2* self, int fs, const double2* psi, int fp, uint64_t len, const double* c,
+                  cudaStream_t stream) {
+    const double2 c0 = make_double2(c[0], c[1]), c1 = make_double2(c[2], c[3]);
+    const unsigned g = flat_grid(len);
+    switch ((fs << 1) | fp) {
+    case 0: linear_kernel<AccF64, AccF64><<<g, 256, 0, stream>>>(self, psi, len, c0, c1); break;
+    case 1: linear_kernel<AccF64, AccDF64><<<g, 256, 0, stream>>>(self, psi, len, c0, c1); break;
+    case 2: linear_kernel<AccDF64, AccF64><<<g, 256, 0, stream>>>(self, psi, len, c0, c1); break;
+    default: linear_kernel<AccDF64, AccDF64><<<g, 256, 0, stream>>>(self, psi, len, c0, c1); break;
+    }
+    QVNT_CUDA_TRY(cudaGetLastError());
+    return QVNT_OK;
+}
 
 int launch_convert_fmt(const double2* src, int fsrc, double2* dst, int fdst, uint64_t len, cudaStream_t stream) {
     if (fsrc == FMT_DF64) convert_from<AccDF64>(src, dst, fdst, len, stream);

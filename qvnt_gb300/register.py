@@ -249,6 +249,35 @@ class QReg:
         check(lib().qvnt_reg_get_polar(self.h, out.ctypes.data))
         return out
 
+    def sample_all(self, count, normals=None, seed=None):
+        """`Reg::sample_all(count)` (quant.rs:513-594): histogram of `count` measurements without
+        collapse.  `normals`: 2^n standard normal draws (qvnt's thread_rng draws); without them the
+        device draws from `seed` (random when None)."""
+        out = np.zeros(1 << self.q_num, dtype=np.uint64)
+        z = None
+        if normals is not None:
+            z = np.ascontiguousarray(normals, dtype=np.float64)
+            assert z.size == out.size
+        if seed is None:
+            seed = _rng.getrandbits(64)
+        check(lib().qvnt_reg_sample_all(self.h, count, seed, z.ctypes.data if z is not None else None,
+                                        out.ctypes.data))
+        return out
+
+    @staticmethod
+    def combine_with_unitary(a, b, c):
+        """`Reg::combine_with_unitary((a, b), c)` (quant.rs:273-308); c: 2x2 complex, row-major."""
+        m = (ctypes.c_double * 8)(*[v for z in c for v in (complex(z).real, complex(z).imag)])
+        h = ctypes.c_void_p()
+        check(lib().qvnt_reg_combine_with_unitary(a.h, b.h, m, ctypes.byref(h)))
+        return QReg._wrap(h, a.q_num + 1, a.ctx)
+
+    def linear_composition(self, other, c0, c1):
+        """`Reg::linear_composition(psi, (c0, c1))` (quant.rs:311-328): self = self c0 + other c1."""
+        m = (ctypes.c_double * 4)(complex(c0).real, complex(c0).imag, complex(c1).real, complex(c1).imag)
+        check(lib().qvnt_reg_linear_composition(self.h, other.h, m))
+        return self
+
     def overlap(self, other):
         """(fidelity |<self|other>|^2 / (<self|self> <other|other>), max |self_i - other_i|), in FP64."""
         f, m = ctypes.c_double(), ctypes.c_double()

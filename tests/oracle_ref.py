@@ -35,6 +35,9 @@ _PROTOS = {
     "oracle_reset_by_mask": (None, [c_void, c_u64, c_u32, c_u64]),
     "oracle_get_polar": (None, [c_void, c_u32, c_void]),
     "oracle_tensor": (None, [c_void, c_u32, c_void, c_u32, c_void]),
+    "oracle_sample_all": (c_int, [c_void, c_u64, c_u32, c_u64, c_void, c_void]),
+    "oracle_combine_with_unitary": (None, [c_void, c_void, c_u32, P(c_double), c_void]),
+    "oracle_linear_composition": (None, [c_void, c_void, c_u64, P(c_double)]),
     "oracle_gate_make": (c_int, [c_u32, c_u64, c_u64, c_double, P(c_double), P(QvntGate)]),
     "oracle_is_unitary_m1": (c_int, [P(c_double)]),
     "oracle_is_unitary_m2": (c_int, [P(c_double)]),
@@ -185,6 +188,27 @@ def tensor(a, na, b, nb):
     out = np.empty(reg_len(na + nb), dtype=np.complex128)
     lib().oracle_tensor(a.ctypes.data, na, b.ctypes.data, nb, out.ctypes.data)
     return out
+
+
+def sample_all(psi, n, count, z):
+    """Histogram of `count` (2^n entries) given the standard-normal draws z; None where qvnt panics."""
+    out = np.zeros(1 << n, dtype=np.uint64)
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    st = lib().oracle_sample_all(psi.ctypes.data, psi.size, n, count, z.ctypes.data, out.ctypes.data)
+    return None if st else out
+
+
+def combine_with_unitary(a, b, n, c):
+    out = np.empty(reg_len(n + 1), dtype=np.complex128)
+    m = (ctypes.c_double * 8)(*[v for z in c for v in (complex(z).real, complex(z).imag)])
+    lib().oracle_combine_with_unitary(a.ctypes.data, b.ctypes.data, n, m, out.ctypes.data)
+    return out
+
+
+def linear_composition(psi, other, c0, c1):
+    m = (ctypes.c_double * 4)(complex(c0).real, complex(c0).imag, complex(c1).real, complex(c1).imag)
+    lib().oracle_linear_composition(psi.ctypes.data, other.ctypes.data, psi.size, m)
+    return psi
 
 
 def max_threads():

@@ -155,3 +155,38 @@ def test_normalize_thresholds():
     psi = np.full(8, 0.25 + 0j)
     orc.normalize(psi, 3)
     assert np.isclose(np.sum(np.abs(psi) ** 2), 1.0)
+
+
+def test_oracle_sample_all_invariants():
+    """sample_all keeps the total at `count` for deficits and excesses, and panics (None) below 3
+    qubits as qvnt does."""
+    import numpy as np
+
+    import oracle_ref as orc
+
+    n = 5
+    rng = np.random.default_rng(1)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    for count in (1, 7, 1000, 123457):
+        for seed in range(4):
+            z = np.random.default_rng(seed).normal(size=1 << n) * (10.0 if seed == 3 else 1.0)
+            out = orc.sample_all(psi.astype(np.complex128), n, count, z)
+            assert int(out.sum()) == count
+    assert orc.sample_all(orc.new_state(2, 0), 2, 10, np.zeros(4)) is None
+
+
+def test_oracle_linear_and_combine():
+    import numpy as np
+
+    import oracle_ref as orc
+
+    rng = np.random.default_rng(3)
+    a = rng.normal(size=16) + 1j * rng.normal(size=16)
+    b = rng.normal(size=16) + 1j * rng.normal(size=16)
+    lin = orc.linear_composition(a.copy(), b, 0.3 - 0.1j, 1.2j)
+    assert np.allclose(lin, a * (0.3 - 0.1j) + b * 1.2j, atol=1e-15)
+    h = 2 ** -0.5
+    c = [h, h, h, -h]
+    out = orc.combine_with_unitary(a, b, 4, c)
+    assert np.allclose(out[:16], h * a + h * b) and np.allclose(out[16:], h * a - h * b)
