@@ -22,7 +22,9 @@
 // states unnormalised).  Norms, probabilities and measurement run in FP64 (measure.cu).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "atomic.cuh"
@@ -144,6 +146,26 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b
         "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
         : "memory");
 }
+// Same MMA with the A operand read from tensor memory (lane = row, one column per TF32 element).
+__device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+// 16 consecutive columns of this thread's lane.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
                  : "memory");
@@ -166,15 +188,19 @@ __device__ __forceinline__ float tf32_rna(float x) {
     return __uint_as_float(r);
 }
 
+// A_TMEM: the TF32 hi/lo operand A lives in tensor memory (written with tcgen05.st, columns 64..191
+// next to the accumulator's 0..63) instead of shared memory.
+template <bool A_TMEM>
 __global__ void __launch_bounds__(kNT, 1)
     precision_tc_kernel(float2* __restrict__ psi, const float* __restrict__ wts, const __grid_constant__ PPassParams P,
                         int* __restrict__ err) {
+    constexpr uint32_t kCols = A_TMEM ? 256 : kTmemCols;
     extern __shared__ __align__(1024) unsigned char smem[];
     // two tile buffers: the next tile's load overlaps the current tile's blocks
     float2* tiles = reinterpret_cast<float2*>(smem);
     float* a_hi = reinterpret_cast<float*>(smem + 2 * kSmemTile);
     float* a_lo = reinterpret_cast<float*>(smem + 2 * kSmemTile + kSmemA);
-    float* w_sm = reinterpret_cast<float*>(smem + 2 * kSmemTile + 2 * kSmemA);
+    float* w_sm = reinterpret_cast<float*>(smem + 2 * kSmemTile + (A_TMEM ? 0 : 2 * kSmemA));
     __shared__ uint64_t seg_off[1 << (kPT - kBQ)];
     __shared__ uint32_t mpos[kMaxPB][128];
     __shared__ uint32_t rpos[kMaxPB][kBD];
@@ -216,7 +242,7 @@ __global__ void __launch_bounds__(kNT, 1)
         for (uint32_t i = tid; i < 2 * kWFloats / 4; i += kNT) dst[i] = __ldg(src + i);
     }
     if (warp == 0) {
-        tmem_alloc(&tmem_base, kTmemCols);
+        tmem_alloc(&tmem_base, kCols);
         tmem_relinquish();
     }
     if (tid == 0) {
@@ -272,11 +298,30 @@ __global__ void __launch_bounds__(kNT, 1)
             load_tile(t + gridDim.x, cur ^ 1u);
         }
         for (uint32_t b = 0; b < nb; ++b) {
+            if constexpr (A_TMEM) {
+                // warp w writes rows 32 (w % 4) .. + 31 (its lane quadrant), columns 16 (w / 4) .. + 15
+                // of A_hi and A_lo: amplitudes r = 8 (w / 4) .. + 7 of its row
+                const uint32_t m = 32u * (warp & 3u) + lane;
+                const uint32_t mp = mpos[b][m];
+                uint32_t hv[16], lv[16];
+#pragma unroll
+                for (uint32_t j = 0; j < 8; ++j) {
+                    const float2 x = tile[mp + rpos[b][8u * (warp >> 2) + j]];
+                    const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
+                    hv[2 * j] = __float_as_uint(hr);
+                    hv[2 * j + 1] = __float_as_uint(hm);
+                    lv[2 * j] = __float_as_uint(x.x - hr);
+                    lv[2 * j + 1] = __float_as_uint(x.y - hm);
+                }
+                const uint32_t row = (32u * (warp & 3u)) << 16;
+                tmem_st16(tmem + row + 64u + 16u * (warp >> 2), hv);
+                tmem_st16(tmem + row + 128u + 16u * (warp >> 2), lv);
+                tmem_st_wait();
+            } else {
             // A[m][2r + c] = component c of the tile amplitude (m, r), split into TF32 hi and lo.
             // Element i = tid + 512 j: row m = tid bits 0-2 and 5-8 (fixed per thread), amplitude
             // r = tid bits 3-4 | j << 2, so both addresses are a per-thread base plus a per-j
             // constant; a warp covers 8 rows x 4 amplitudes (64-bit stores in two wavefronts).
-            {
                 const uint32_t m = (tid & 7u) | ((tid >> 5) << 3);
                 const uint32_t rlo = (tid >> 3) & 3u;
                 const uint32_t tb = mpos[b][m] + rpos[b][rlo];
@@ -288,23 +333,33 @@ __global__ void __launch_bounds__(kNT, 1)
                     *reinterpret_cast<float2*>(a_hi + ab + 64 * j) = make_float2(hr, hm);
                     *reinterpret_cast<float2*>(a_lo + ab + 64 * j) = make_float2(x.x - hr, x.y - hm);
                 }
+                fence_proxy_async();
             }
-            fence_proxy_async();
             tc_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc_after_sync();
-                const uint32_t ah = smem_addr(a_hi), al = smem_addr(a_lo);
                 const uint32_t wh = smem_addr(w_sm + (size_t)b * 2 * kWFloats), wl = wh + kWFloats * 4;
-                const uint32_t as[3] = {al, ah, ah};
                 const uint32_t bs[3] = {wh, wl, wh};
                 uint32_t acc = 0;
-                for (int term = 0; term < 3; ++term)
+                if constexpr (A_TMEM) {
+                    const uint32_t as[3] = {tmem + 128u, tmem + 64u, tmem + 64u};  // lo, hi, hi
+                    for (int term = 0; term < 3; ++term)
 #pragma unroll
-                    for (uint32_t ks = 0; ks < 8; ++ks) {
-                        mma_tf32(tmem, smem_desc(as[term] + ks * 256u), smem_desc(bs[term] + ks * 256u), acc);
-                        acc = 1;
-                    }
+                        for (uint32_t ks = 0; ks < 8; ++ks) {
+                            mma_tf32_ta(tmem, as[term] + ks * 8u, smem_desc(bs[term] + ks * 256u), acc);
+                            acc = 1;
+                        }
+                } else {
+                    const uint32_t ah = smem_addr(a_hi), al = smem_addr(a_lo);
+                    const uint32_t as[3] = {al, ah, ah};
+                    for (int term = 0; term < 3; ++term)
+#pragma unroll
+                        for (uint32_t ks = 0; ks < 8; ++ks) {
+                            mma_tf32(tmem, smem_desc(as[term] + ks * 256u), smem_desc(bs[term] + ks * 256u), acc);
+                            acc = 1;
+                        }
+                }
                 mma_commit(&bar_mma);
             }
             if (!mbar_wait(&bar_mma, ph_mma)) {
@@ -347,7 +402,7 @@ __global__ void __launch_bounds__(kNT, 1)
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0) tmem_dealloc(tmem, kCols);
 }
 
 // ---- host: dense gate matrices, blocks, passes ----------------------------------------------------
@@ -506,17 +561,31 @@ struct PPlan {
     std::vector<size_t> members;  // block indices
 };
 
-void make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan>& passes) {
+// Lowest qubits every pass keeps in its tile: 2^lowq contiguous amplitudes per TMA copy.  At most
+// 12 - 5 = 7, so that a block on five other qubits still fits an empty tile.  Longer runs cost passes
+// but make each pass faster (fewer, larger copies with better DRAM locality); measured at 30 qubits,
+// depth 60: lowq 5 -> 262 passes of 10.9 ms, 6 -> 310 of 7.7 ms, 7 -> 345 of 6.5 ms.
+// QVNT_PRECISION_LOWQ (5..7) overrides the default of 7.
+uint32_t precision_lowq() {
+    static const uint32_t v = [] {
+        const char* e = std::getenv("QVNT_PRECISION_LOWQ");
+        const int x = e ? std::atoi(e) : 0;
+        return (uint32_t)(x >= 5 && x <= kPT - kBQ ? x : kPT - kBQ);
+    }();
+    return v;
+}
+
+int make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan>& passes) {
     passes.clear();
     const size_t n = blocks.size();
     std::vector<char> done(n, 0);
     size_t first = 0;
-    const uint64_t low = (1ull << kBQ) - 1ull;
+    const uint64_t low = (1ull << precision_lowq()) - 1ull;
     while (true) {
         while (first < n && done[first]) ++first;
         if (first >= n) break;
         PPlan p;
-        uint64_t Q = low, blocked = 0;
+        uint64_t Q = low & ((L >= 64) ? ~0ull : ((1ull << L) - 1ull)), blocked = 0;
         size_t scanned = 0;
         for (size_t j = first; j < n && scanned < 64 && p.members.size() < (size_t)kMaxPB; ++j) {
             if (done[j]) continue;
@@ -530,10 +599,13 @@ void make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan
                 blocked |= S;
             }
         }
+        if (p.members.empty())  // cannot happen with lowq <= 7: a block always fits an empty tile
+            return set_error(QVNT_ERR_UNSUPPORTED, "precision planner could not place block %zu", first);
         for (uint32_t q = 0; q < L && __builtin_popcountll(Q) < kPT; ++q) Q |= 1ull << q;
         p.qmask = Q;
         passes.push_back(std::move(p));
     }
+    return QVNT_OK;
 }
 
 // TF32 rounding to nearest (ties away from zero), as cvt.rna.tf32.f32 does on the device.
@@ -579,7 +651,8 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     std::vector<Block> blocks;
     make_blocks(lg, L, blocks);
     std::vector<PPlan> passes;
-    make_passes(blocks, L, passes);
+    st = make_passes(blocks, L, passes);
+    if (st) return st;
     // weights of every block, uploaded once per apply call
     const size_t wfl = blocks.size() * 2 * kWFloats;
     FusedState& fs = r->fused;
@@ -597,9 +670,19 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     double* d_norm0 = reinterpret_cast<double*>(r->d_small) + 5;
     double* d_norm = reinterpret_cast<double*>(r->d_small) + 6;
     TRY_LAUNCH(launch_norm_sqr_sum(r->psi, r->fmt, r->len, r->scratch, d_norm0, r->stream));
+    // operand A in tensor memory (default) or in shared memory (QVNT_PRECISION_A=smem)
+    static const bool a_tmem = [] {
+        const char* e = std::getenv("QVNT_PRECISION_A");
+        return !(e && std::string(e) == "smem");
+    }();
     static const bool attr = [] {
-        return cudaFuncSetAttribute((const void*)precision_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(2 * kSmemTile + 2 * kSmemA + kMaxPB * kSmemW)) == cudaSuccess;
+        const bool a = cudaFuncSetAttribute((const void*)precision_tc_kernel<false>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)(2 * kSmemTile + 2 * kSmemA + kMaxPB * kSmemW)) == cudaSuccess;
+        const bool b = cudaFuncSetAttribute((const void*)precision_tc_kernel<true>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)(2 * kSmemTile + kMaxPB * kSmemW)) == cudaSuccess;
+        return a && b;
     }();
     if (!attr) return set_error(QVNT_ERR_CUDA, "precision kernel: shared-memory attribute refused");
     int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
@@ -627,14 +710,18 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
                 if ((b.sup >> q) & 1ull) P.blocks[j].bits[jj++] = (uint8_t)pos_of[q];
             P.blocks[j].w_off = (uint32_t)(p.members[j] * 2 * kWFloats);
         }
-        const size_t smem = 2 * kSmemTile + 2 * kSmemA + P.nblocks * kSmemW;
+        const size_t smem = 2 * kSmemTile + (a_tmem ? 0 : 2 * kSmemA) + P.nblocks * kSmemW;
         uint64_t grid = (uint64_t)r->ctx->geo.sms;
         if (grid > P.ntiles) grid = P.ntiles;
         cudaEvent_t stop = nullptr;
         st = timing_begin(r, &stop);
         if (st) return st;
-        precision_tc_kernel<<<(unsigned)grid, kNT, smem, r->stream>>>(reinterpret_cast<float2*>(r->psi),
-                                                                        static_cast<const float*>(fs.d_buf), P, d_err);
+        if (a_tmem)
+            precision_tc_kernel<true><<<(unsigned)grid, kNT, smem, r->stream>>>(
+                reinterpret_cast<float2*>(r->psi), static_cast<const float*>(fs.d_buf), P, d_err);
+        else
+            precision_tc_kernel<false><<<(unsigned)grid, kNT, smem, r->stream>>>(
+                reinterpret_cast<float2*>(r->psi), static_cast<const float*>(fs.d_buf), P, d_err);
         QVNT_CUDA_TRY(cudaGetLastError());
         st = timing_end(r, stop);
         if (st) return st;
@@ -657,7 +744,8 @@ int precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64
     std::vector<Block> bl;
     make_blocks(lg, L, bl);
     std::vector<PPlan> ps;
-    make_passes(bl, L, ps);
+    st = make_passes(bl, L, ps);
+    if (st) return st;
     *passes = ps.size();
     *blocks = bl.size();
     return QVNT_OK;

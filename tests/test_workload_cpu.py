@@ -39,3 +39,18 @@ def test_batch_workload_shape():
         for j in range(cnt):
             g = ptr[j]
             assert (lib().qvnt_gate_act_on(ptr[j]) | g.ctrl) < lim
+
+
+@pytest.mark.parametrize("n", [12, 13, 16, 24, 32])
+def test_precision_planner_terminates(n):
+    """The precision engine's host planner places every dense block (it fuses the config-3 layers
+    at about ten gates per block)."""
+    import ctypes
+
+    from qvnt_gb300._abi import check, lib
+    from qvnt_gb300.circuits import SplitMix64, random_layers_gates
+
+    arr, cnt = random_layers_gates(n, 12, SplitMix64(n))
+    p, b = ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().qvnt_precision_plan_info(arr, cnt, n, ctypes.byref(p), ctypes.byref(b)))
+    assert 0 < b.value <= cnt and 0 < p.value <= b.value
