@@ -23,6 +23,9 @@ import argparse
 import ctypes
 import json
 import os
+
+# 32 hardware work queues for the serving form's concurrent streams; must precede CUDA initialisation
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import subprocess
 import sys
 import threading
@@ -297,14 +300,14 @@ def bench_precision(ctx, n=32, depth=60, n_ref=30):
 
 def bench_serve(ctx, rate, seconds):
     """Serving form: Poisson arrivals at `rate`/s for `seconds` s (n log-uniform [10, 28], depth
-    uniform [5, 100] over 1-3 apply/measure rounds, 150 GB HBM budget, 128 slots, queue of 1024);
+    uniform [5, 100] over 1-3 apply/measure rounds, 150 GB HBM budget, 32 slots, queue of 1024);
     then 5 s to drain.  Latency = completion - scheduled arrival."""
     import numpy as np
     from qvnt_gb300.circuits import serve_requests
     from qvnt_gb300.serve import Server
 
     max_queue = 1024
-    s = Server(budget_bytes=150 * 10**9, slots=128, max_queue=max_queue, ctx=ctx)
+    s = Server(budget_bytes=150 * 10**9, slots=32, max_queue=max_queue, ctx=ctx)
     t0 = s.clock()
     offered = shed = 0
     for r in serve_requests(rate=rate, duration=seconds, seed=5):
@@ -327,7 +330,7 @@ def bench_serve(ctx, rate, seconds):
     pct = (lambda a, p: float(np.percentile(a, p)) * 1e3 if a.size else None)
     censored = np.concatenate([lat, ages]) if ages.size else lat
     return {"workload": "Poisson %.0f req/s for %.0f s, n log-uniform [10, 28], depth uniform [5, 100], "
-                        "1-3 apply/measure rounds, 150 GB budget, 128 slots, queue 1024" % (rate, seconds),
+                        "1-3 apply/measure rounds, 150 GB budget, 32 slots, queue 1024" % (rate, seconds),
             "offered": offered, "submitted": st["submitted"], "shed": shed, "completed": st["completed"],
             "failed": st["failed"], "queued_at_end": st["queued"], "running_at_end": st["running"],
             "served_circuits_per_s": st["completed"] / elapsed, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99),

@@ -362,6 +362,9 @@ int qvnt_batch_info(const qvnt_batch* batch, uint64_t* items, uint64_t* passes, 
  *                        of the requests still queued.
  *   qvnt_server_destroy  finishes the running requests, fails the queued ones; no wait may be in
  *                        progress on another thread.
+ * Each slot drives its own CUDA stream: give the process at least as many hardware work queues as
+ * slots (CUDA_DEVICE_MAX_CONNECTIONS, at most 32; qvnt_ctx_create sets 32 unless the variable is
+ * set), or the kernels of small requests wait in FIFO order behind those of large ones.
  * ------------------------------------------------------------------------------------------- */
 #define QVNT_CALL_APPLY 0u
 #define QVNT_CALL_MEASURE 1u

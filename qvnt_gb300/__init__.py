@@ -9,7 +9,14 @@ The state vector lives only in GPU memory; every gate, reduction and measurement
 library's CUDA kernels (qvnt_gb300/csrc/).  This package is the Python side of the C ABI in
 include/qvnt_gb300.h.
 """
-from . import operator as op
+import os as _os
+
+# Independent registers run on independent CUDA streams; 32 hardware work queues (instead of the
+# default 8) keep their kernels from serialising behind each other.  Read when the process creates
+# its CUDA context, so it must be set before any CUDA use (e.g. by torch).
+_os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
+from . import operator as op  # noqa: E402
 from ._abi import ENGINE_FUSED, ENGINE_PLAIN, ENGINE_PRECISION, KIND, KINDS, MaskError, QvntError, QvntGate
 from .operator import MultiOp, SingleOp
 from .register import Context, CReg, QReg, VReg, bits_iter, default_context

@@ -5,6 +5,7 @@
 // max(2^n, 8) Complex<f64> amplitudes (16 B each, interleaved), owned by the library.
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -329,6 +330,10 @@ uint32_t qvnt_abi_version(void) { return (1u << 16) | 0u; }
 
 int qvnt_ctx_create(int device, qvnt_ctx** out) {
     if (!out) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
+    // Registers run on their own streams; with the default 8 hardware work queues the kernels of many
+    // concurrent registers (the serving loop) serialise in FIFO order behind each other.  32 queues,
+    // unless the host set a value; effective only if no CUDA context exists yet in this process.
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     int ndev = 0;
     QVNT_CUDA_TRY(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev) return set_error(QVNT_ERR_BAD_ARG, "device %d not present (%d)", device, ndev);
