@@ -5,16 +5,19 @@
 // into one-qubit factors for the multi-bit X/Y/Z/S/T of src/operator/atomic/{x,y,z,s,t}.rs), then
 // greedily fuses gates into BLOCKS of at most five qubits (a gate may overtake earlier skipped
 // gates only when their supports are disjoint), multiplying their matrices in double precision.
-// Blocks are grouped into PASSES: a pass picks 12 tile qubits (the 5 lowest, so a tile is a set of
-// 256-byte runs, plus the qubits of up to kMaxPB blocks) and each CTA, persistent over tiles:
-//   1. stages the tile (4096 amplitudes, 32 KB) into shared memory with TMA bulk copies, the next
+// Blocks are grouped into PASSES: a pass picks 13 tile qubits (12 for a 12-qubit register): the 7
+// lowest, so a tile is a set of 1 KB runs, plus the qubits of up to kMaxPB blocks.  Each CTA,
+// persistent over tiles:
+//   1. stages the tile (8192 amplitudes, 64 KB) into shared memory with TMA bulk copies, the next
 //      tile's copies running into a second buffer while this one is processed;
-//   2. per block: threads repack the tile into the MMA operand A (128 rows = the 7 other tile bits,
-//      64 columns = the block's 32 amplitudes as (re, im)), split into TF32 hi and lo parts;
-//      one thread issues D = A_lo W_hi^T + A_hi W_lo^T + A_hi W_hi^T as 24 tcgen05.mma (kind::tf32,
-//      M = 128, N = 64, K = 8) into a 128 x 64 FP32 accumulator in tensor memory, where W is the
-//      block's unitary as a real 64 x 64 matrix ([[Re, -Im], [Im, Re]] interleaved), kept in shared
-//      memory for the whole pass; threads read D back with tcgen05.ld and scatter it into the tile;
+//   2. per block: threads repack the tile into the MMA operand A (2 x 128 rows = the 8 other tile
+//      bits, 64 columns = the block's 32 amplitudes as (re, im)), split into TF32 hi and lo parts and
+//      written to tensor memory with tcgen05.st; one thread issues, per 128-row half,
+//      D = A_lo W_hi^T + A_hi W_lo^T + A_hi W_hi^T as 24 tcgen05.mma (kind::tf32, M = 128, N = 64,
+//      K = 8, A from tensor memory, B from shared memory) into a 128 x 64 FP32 accumulator in tensor
+//      memory, where W is the block's unitary as a real 64 x 64 matrix ([[Re, -Im], [Im, Re]]
+//      interleaved), kept in shared memory for the whole pass; threads read D back with tcgen05.ld
+//      and scatter it into the tile;
 //   3. writes the tile back with TMA bulk stores.
 // The three-term TF32 split keeps each block product at ~2^-21 relative error with FP32
 // accumulation.  Every kRenormEvery passes the state is rescaled in FP64 to the norm it had when
@@ -41,16 +44,17 @@ namespace qvnt {
 
 namespace {
 
-constexpr int kPT = 12;            // tile qubits
+constexpr int kPT = 13;            // tile qubits (at most; 12 for a 12-qubit register)
 constexpr int kBQ = 5;             // block qubits
 constexpr int kBD = 1 << kBQ;      // block dimension
 constexpr int kNT = 512;           // threads: 16 warps, four per tensor-memory lane quadrant
 constexpr int kMaxPB = 2;          // blocks per pass (their weights stay in shared memory)
 constexpr int kRenormEvery = 10;   // passes between FP64 norm restorations
 constexpr uint32_t kPWaitLimit = 1u << 22;
-constexpr uint32_t kTmemCols = 64;
 constexpr uint32_t kWFloats = 64 * 64;  // one weight matrix (hi or lo)
-constexpr size_t kSmemTile = 32768, kSmemA = 32768, kSmemW = 2 * kWFloats * 4;
+constexpr uint32_t kTileAmps = 1u << kPT;
+constexpr uint32_t kMaxRows = 1u << (kPT - kBQ);
+constexpr size_t kSmemTile = (size_t)kTileAmps * 8, kSmemW = 2 * kWFloats * 4;
 
 // Operand layout of tcgen05 for a K-major matrix without swizzling: core matrices of 8 rows x 16
 // bytes (row stride 16 B); the 16 core matrices along K (64 floats) of an 8-row group are contiguous
@@ -138,15 +142,8 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
 // Instruction descriptor of kind::tf32: FP32 accumulator, A and B TF32 and K-major, N = 64, M = 128.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-        : "memory");
-}
-// Same MMA with the A operand read from tensor memory (lane = row, one column per TF32 element).
+// D (+)= A * B^T with A in tensor memory (lane = row, one column per TF32 element) and B in shared
+// memory.
 __device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -188,21 +185,22 @@ __device__ __forceinline__ float tf32_rna(float x) {
     return __uint_as_float(r);
 }
 
-// A_TMEM: the TF32 hi/lo operand A lives in tensor memory (written with tcgen05.st, columns 64..191
-// next to the accumulator's 0..63) instead of shared memory.
-template <bool A_TMEM>
+// One pass.  A tile holds 2^k amplitudes (k = 12 or 13): 2^(k-5) operand rows in halves of 128 (the
+// MMA's M); per block and half, the TF32 hi/lo operand A is written to tensor memory with tcgen05.st
+// (lanes = rows, one column per element) next to that half's accumulator:
+//   columns   0..127  D of half 0 / 1 (64 each)
+//   columns 128..255  A_hi of half 0 / 1
+//   columns 256..383  A_lo of half 0 / 1
 __global__ void __launch_bounds__(kNT, 1)
     precision_tc_kernel(float2* __restrict__ psi, const float* __restrict__ wts, const __grid_constant__ PPassParams P,
                         int* __restrict__ err) {
-    constexpr uint32_t kCols = A_TMEM ? 256 : kTmemCols;
+    constexpr uint32_t kCols = 512;
     extern __shared__ __align__(1024) unsigned char smem[];
     // two tile buffers: the next tile's load overlaps the current tile's blocks
     float2* tiles = reinterpret_cast<float2*>(smem);
-    float* a_hi = reinterpret_cast<float*>(smem + 2 * kSmemTile);
-    float* a_lo = reinterpret_cast<float*>(smem + 2 * kSmemTile + kSmemA);
-    float* w_sm = reinterpret_cast<float*>(smem + 2 * kSmemTile + (A_TMEM ? 0 : 2 * kSmemA));
+    float* w_sm = reinterpret_cast<float*>(smem + 2 * kSmemTile);
     __shared__ uint64_t seg_off[1 << (kPT - kBQ)];
-    __shared__ uint32_t mpos[kMaxPB][128];
+    __shared__ uint32_t mpos[kMaxPB][kMaxRows];
     __shared__ uint32_t rpos[kMaxPB][kBD];
     __shared__ __align__(8) uint64_t bar_tma[2];
     __shared__ __align__(8) uint64_t bar_mma;
@@ -212,6 +210,9 @@ __global__ void __launch_bounds__(kNT, 1)
     const uint32_t k = P.k, c = P.c, nb = P.nblocks;
     const uint32_t nseg = 1u << (k - c);
     const uint32_t seg_amps = 1u << c;
+    const uint32_t rows = 1u << (k - kBQ);   // 128 or 256
+    const uint32_t halves = rows >> 7;
+    const uint32_t tile_amps = 1u << k;
 
     for (uint32_t s = tid; s < nseg; s += kNT) {
         uint64_t off = 0;
@@ -222,9 +223,9 @@ __global__ void __launch_bounds__(kNT, 1)
     for (uint32_t b = 0; b < nb; ++b) {
         uint32_t bm = 0;
         for (int j = 0; j < kBQ; ++j) bm |= 1u << P.blocks[b].bits[j];
-        if (tid < 128) {  // the 7 other tile bits carry the operand row m
+        if (tid < rows) {  // the other tile bits carry the operand row m
             uint32_t pos = 0, bit = 0;
-            for (uint32_t p = 0; p < (uint32_t)kPT; ++p) {
+            for (uint32_t p = 0; p < k; ++p) {
                 if ((bm >> p) & 1u) continue;
                 if ((tid >> bit) & 1u) pos |= 1u << p;
                 ++bit;
@@ -265,10 +266,10 @@ __global__ void __launch_bounds__(kNT, 1)
     // warp 0 issues the bulk copies of one tile into buffer `buf`
     auto load_tile = [&](uint64_t t, uint32_t buf) {
         const uint64_t base = tile_base(t);
-        float2* tile = tiles + (size_t)buf * 4096;
+        float2* tile = tiles + (size_t)buf * kTileAmps;
         if (lane == 0) {
             fence_proxy_async();
-            mbar_expect_tx(&bar_tma[buf], (1u << k) * 8u);
+            mbar_expect_tx(&bar_tma[buf], tile_amps * 8u);
         }
         __syncwarp();
         for (uint32_t s = lane; s < nseg; s += 32)
@@ -280,12 +281,14 @@ __global__ void __launch_bounds__(kNT, 1)
     __syncthreads();
     tc_after_sync();
     const uint32_t tmem = tmem_base;
+    const uint32_t lane_base = (32u * (warp & 3u)) << 16;  // this warp's tensor-memory lane quadrant
+    const uint32_t grp = warp >> 2;                       // column group: amplitudes 8 grp .. + 7
     uint32_t ph_tma[2] = {0, 0};
     uint32_t ph_mma = 0;
     uint32_t it = 0;
     for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x, ++it) {
         const uint32_t cur = it & 1u;
-        float2* tile = tiles + (size_t)cur * 4096;
+        float2* tile = tiles + (size_t)cur * kTileAmps;
         if (!mbar_wait(&bar_tma[cur], ph_tma[cur])) {
             atomicExch(err, 1);
             s_abort = 1;
@@ -298,65 +301,39 @@ __global__ void __launch_bounds__(kNT, 1)
             load_tile(t + gridDim.x, cur ^ 1u);
         }
         for (uint32_t b = 0; b < nb; ++b) {
-            if constexpr (A_TMEM) {
-                // warp w writes rows 32 (w % 4) .. + 31 (its lane quadrant), columns 16 (w / 4) .. + 15
-                // of A_hi and A_lo: amplitudes r = 8 (w / 4) .. + 7 of its row
-                const uint32_t m = 32u * (warp & 3u) + lane;
+            // warp w writes rows 32 (w % 4) .. + 31 of each half (its lane quadrant), columns
+            // 16 (w / 4) .. + 15 of A_hi and A_lo: amplitudes r = 8 (w / 4) .. + 7 of the row
+            for (uint32_t h = 0; h < halves; ++h) {
+                const uint32_t m = 128u * h + 32u * (warp & 3u) + lane;
                 const uint32_t mp = mpos[b][m];
                 uint32_t hv[16], lv[16];
 #pragma unroll
                 for (uint32_t j = 0; j < 8; ++j) {
-                    const float2 x = tile[mp + rpos[b][8u * (warp >> 2) + j]];
+                    const float2 x = tile[mp + rpos[b][8u * grp + j]];
                     const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
                     hv[2 * j] = __float_as_uint(hr);
                     hv[2 * j + 1] = __float_as_uint(hm);
                     lv[2 * j] = __float_as_uint(x.x - hr);
                     lv[2 * j + 1] = __float_as_uint(x.y - hm);
                 }
-                const uint32_t row = (32u * (warp & 3u)) << 16;
-                tmem_st16(tmem + row + 64u + 16u * (warp >> 2), hv);
-                tmem_st16(tmem + row + 128u + 16u * (warp >> 2), lv);
-                tmem_st_wait();
-            } else {
-            // A[m][2r + c] = component c of the tile amplitude (m, r), split into TF32 hi and lo.
-            // Element i = tid + 512 j: row m = tid bits 0-2 and 5-8 (fixed per thread), amplitude
-            // r = tid bits 3-4 | j << 2, so both addresses are a per-thread base plus a per-j
-            // constant; a warp covers 8 rows x 4 amplitudes (64-bit stores in two wavefronts).
-                const uint32_t m = (tid & 7u) | ((tid >> 5) << 3);
-                const uint32_t rlo = (tid >> 3) & 3u;
-                const uint32_t tb = mpos[b][m] + rpos[b][rlo];
-                const uint32_t ab = op_off(m, 2 * rlo);
-#pragma unroll
-                for (uint32_t j = 0; j < 8; ++j) {
-                    const float2 x = tile[tb + rpos[b][4 * j]];
-                    const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
-                    *reinterpret_cast<float2*>(a_hi + ab + 64 * j) = make_float2(hr, hm);
-                    *reinterpret_cast<float2*>(a_lo + ab + 64 * j) = make_float2(x.x - hr, x.y - hm);
-                }
-                fence_proxy_async();
+                tmem_st16(tmem + lane_base + 128u + 64u * h + 16u * grp, hv);
+                tmem_st16(tmem + lane_base + 256u + 64u * h + 16u * grp, lv);
             }
+            tmem_st_wait();
             tc_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc_after_sync();
                 const uint32_t wh = smem_addr(w_sm + (size_t)b * 2 * kWFloats), wl = wh + kWFloats * 4;
                 const uint32_t bs[3] = {wh, wl, wh};
-                uint32_t acc = 0;
-                if constexpr (A_TMEM) {
-                    const uint32_t as[3] = {tmem + 128u, tmem + 64u, tmem + 64u};  // lo, hi, hi
+                for (uint32_t h = 0; h < halves; ++h) {
+                    const uint32_t as[3] = {tmem + 256u + 64u * h, tmem + 128u + 64u * h,
+                                            tmem + 128u + 64u * h};  // lo, hi, hi
+                    uint32_t acc = 0;
                     for (int term = 0; term < 3; ++term)
 #pragma unroll
                         for (uint32_t ks = 0; ks < 8; ++ks) {
-                            mma_tf32_ta(tmem, as[term] + ks * 8u, smem_desc(bs[term] + ks * 256u), acc);
-                            acc = 1;
-                        }
-                } else {
-                    const uint32_t ah = smem_addr(a_hi), al = smem_addr(a_lo);
-                    const uint32_t as[3] = {al, ah, ah};
-                    for (int term = 0; term < 3; ++term)
-#pragma unroll
-                        for (uint32_t ks = 0; ks < 8; ++ks) {
-                            mma_tf32(tmem, smem_desc(as[term] + ks * 256u), smem_desc(bs[term] + ks * 256u), acc);
+                            mma_tf32_ta(tmem + 64u * h, as[term] + ks * 8u, smem_desc(bs[term] + ks * 256u), acc);
                             acc = 1;
                         }
                 }
@@ -368,16 +345,18 @@ __global__ void __launch_bounds__(kNT, 1)
             }
             ph_mma ^= 1u;
             tc_after_sync();
-            // warp w: accumulator lanes 32 (w % 4) .. + 31 (rows m), columns 16 (w / 4) .. + 15
-            uint32_t v[16];
-            tmem_ld16(tmem + ((32u * (warp & 3u)) << 16) + 16u * (warp >> 2), v);
-            tmem_ld_wait();
-            const uint32_t m = 32u * (warp & 3u) + lane;
-            const uint32_t mp = mpos[b][m];
+            // warp w: accumulator lanes of its quadrant (rows m), columns 16 (w / 4) .. + 15
+            for (uint32_t h = 0; h < halves; ++h) {
+                uint32_t v[16];
+                tmem_ld16(tmem + lane_base + 64u * h + 16u * grp, v);
+                tmem_ld_wait();
+                const uint32_t m = 128u * h + 32u * (warp & 3u) + lane;
+                const uint32_t mp = mpos[b][m];
 #pragma unroll
-            for (uint32_t j = 0; j < 8; ++j)
-                tile[mp + rpos[b][8u * (warp >> 2) + j]] = make_float2(__uint_as_float(v[2 * j]),
-                                                                       __uint_as_float(v[2 * j + 1]));
+                for (uint32_t j = 0; j < 8; ++j)
+                    tile[mp + rpos[b][8u * grp + j]] = make_float2(__uint_as_float(v[2 * j]),
+                                                                   __uint_as_float(v[2 * j + 1]));
+            }
             tc_before_sync();
             __syncthreads();
             if (s_abort) break;
@@ -562,7 +541,7 @@ struct PPlan {
 };
 
 // Lowest qubits every pass keeps in its tile: 2^lowq contiguous amplitudes per TMA copy.  At most
-// 12 - 5 = 7, so that a block on five other qubits still fits an empty tile.  Longer runs cost passes
+// 12 - 5 = 7, so that a block on five other qubits still fits an empty tile of a 12-qubit register.  Longer runs cost passes
 // but make each pass faster (fewer, larger copies with better DRAM locality); measured at 30 qubits,
 // depth 60: lowq 5 -> 262 passes of 10.9 ms, 6 -> 310 of 7.7 ms, 7 -> 345 of 6.5 ms.
 // QVNT_PRECISION_LOWQ (5..7) overrides the default of 7.
@@ -570,13 +549,14 @@ uint32_t precision_lowq() {
     static const uint32_t v = [] {
         const char* e = std::getenv("QVNT_PRECISION_LOWQ");
         const int x = e ? std::atoi(e) : 0;
-        return (uint32_t)(x >= 5 && x <= kPT - kBQ ? x : kPT - kBQ);
+        return (uint32_t)(x >= 5 && x <= 7 ? x : 7);
     }();
     return v;
 }
 
 int make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan>& passes) {
     passes.clear();
+    const int kt = std::min<int>(kPT, (int)L);  // tile qubits
     const size_t n = blocks.size();
     std::vector<char> done(n, 0);
     size_t first = 0;
@@ -591,7 +571,7 @@ int make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan>
             if (done[j]) continue;
             ++scanned;
             const uint64_t S = blocks[j].sup;
-            if (!(S & blocked) && __builtin_popcountll(Q | S) <= kPT) {
+            if (!(S & blocked) && __builtin_popcountll(Q | S) <= kt) {
                 Q |= S;
                 p.members.push_back(j);
                 done[j] = 1;
@@ -601,7 +581,7 @@ int make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan>
         }
         if (p.members.empty())  // cannot happen with lowq <= 7: a block always fits an empty tile
             return set_error(QVNT_ERR_UNSUPPORTED, "precision planner could not place block %zu", first);
-        for (uint32_t q = 0; q < L && __builtin_popcountll(Q) < kPT; ++q) Q |= 1ull << q;
+        for (uint32_t q = 0; q < L && __builtin_popcountll(Q) < kt; ++q) Q |= 1ull << q;
         p.qmask = Q;
         passes.push_back(std::move(p));
     }
@@ -642,8 +622,7 @@ void block_weights(const Block& b, float* hi, float* lo) {
 
 int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
-    if (L < (uint32_t)kPT)
-        return set_error(QVNT_ERR_UNSUPPORTED, "the precision engine needs at least %d qubits", kPT);
+    if (L < 12) return set_error(QVNT_ERR_UNSUPPORTED, "the precision engine needs at least 12 qubits");
     std::vector<LGate> lg;
     int st = lower_dense(gates, count, lg);
     if (st) return st;
@@ -670,19 +649,9 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     double* d_norm0 = reinterpret_cast<double*>(r->d_small) + 5;
     double* d_norm = reinterpret_cast<double*>(r->d_small) + 6;
     TRY_LAUNCH(launch_norm_sqr_sum(r->psi, r->fmt, r->len, r->scratch, d_norm0, r->stream));
-    // operand A in tensor memory (default) or in shared memory (QVNT_PRECISION_A=smem)
-    static const bool a_tmem = [] {
-        const char* e = std::getenv("QVNT_PRECISION_A");
-        return !(e && std::string(e) == "smem");
-    }();
     static const bool attr = [] {
-        const bool a = cudaFuncSetAttribute((const void*)precision_tc_kernel<false>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)(2 * kSmemTile + 2 * kSmemA + kMaxPB * kSmemW)) == cudaSuccess;
-        const bool b = cudaFuncSetAttribute((const void*)precision_tc_kernel<true>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)(2 * kSmemTile + kMaxPB * kSmemW)) == cudaSuccess;
-        return a && b;
+        return cudaFuncSetAttribute((const void*)precision_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(2 * kSmemTile + kMaxPB * kSmemW)) == cudaSuccess;
     }();
     if (!attr) return set_error(QVNT_ERR_CUDA, "precision kernel: shared-memory attribute refused");
     int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
@@ -710,18 +679,14 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
                 if ((b.sup >> q) & 1ull) P.blocks[j].bits[jj++] = (uint8_t)pos_of[q];
             P.blocks[j].w_off = (uint32_t)(p.members[j] * 2 * kWFloats);
         }
-        const size_t smem = 2 * kSmemTile + (a_tmem ? 0 : 2 * kSmemA) + P.nblocks * kSmemW;
+        const size_t smem = 2 * kSmemTile + P.nblocks * kSmemW;
         uint64_t grid = (uint64_t)r->ctx->geo.sms;
         if (grid > P.ntiles) grid = P.ntiles;
         cudaEvent_t stop = nullptr;
         st = timing_begin(r, &stop);
         if (st) return st;
-        if (a_tmem)
-            precision_tc_kernel<true><<<(unsigned)grid, kNT, smem, r->stream>>>(
-                reinterpret_cast<float2*>(r->psi), static_cast<const float*>(fs.d_buf), P, d_err);
-        else
-            precision_tc_kernel<false><<<(unsigned)grid, kNT, smem, r->stream>>>(
-                reinterpret_cast<float2*>(r->psi), static_cast<const float*>(fs.d_buf), P, d_err);
+        precision_tc_kernel<<<(unsigned)grid, kNT, smem, r->stream>>>(reinterpret_cast<float2*>(r->psi),
+                                                                        static_cast<const float*>(fs.d_buf), P, d_err);
         QVNT_CUDA_TRY(cudaGetLastError());
         st = timing_end(r, stop);
         if (st) return st;
