@@ -715,14 +715,14 @@ int qvnt_apply_host(qvnt_ctx* ctx, const qvnt_gate* gates, size_t count, const d
         if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
     }
     QVNT_CUDA_TRY(cudaSetDevice(ctx->device));
-    // The plugin register is scratch: its storage is converted in place around the gate passes.
+    // The plugin register is scratch: its storage is converted in place around the gate passes (and
+    // left as IEEE f64 afterwards: the next call overwrites it).
     QVNT_CUDA_TRY(cudaMemcpyAsync(r->psi, psi_i, len * sizeof(amp_t), cudaMemcpyHostToDevice, r->stream));
     if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 1, r->stream));
     TRY(r->engine == QVNT_ENGINE_PLAIN ? apply_plain(r, gates, count) : apply_fused(r, gates, count));
     if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 0, r->stream));
     QVNT_CUDA_TRY(cudaMemcpyAsync(psi_o, r->psi, len * sizeof(amp_t), cudaMemcpyDeviceToHost, r->stream));
-    if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 1, r->stream));
-    r->launches += r->fmt == FMT_DF64 ? 3 : 0;
+    r->launches += r->fmt == FMT_DF64 ? 2 : 0;
     return reg_sync(r);
 }
 
