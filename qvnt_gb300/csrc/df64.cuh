@@ -133,14 +133,50 @@ __device__ __forceinline__ dfc dfc_rotate(dfc z, uint32_t q) {
     return z;
 }
 
-// ---- conversions (FP64 path: only at API boundaries and in register-wide passes) ---------------
+// ---- conversions (only at API boundaries and in register-wide passes) -----------------------------
+// On the device the float <-> double conversions are done on the bit patterns with integer
+// instructions: GB300 converts between the two formats far more slowly than it issues integer ops.
+// Results are those of the IEEE conversions (round to nearest even); zeros, subnormals, overflow,
+// infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ float d2f_rn_bits(double x) {
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(u >> 32) & 0x80000000u;
+    const int fe = (int)((u >> 52) & 0x7ffu) - 1023 + 127;
+    if (fe <= 0 || fe >= 255) return __double2float_rn(x);
+    const uint32_t top = (uint32_t)((u >> 29) & 0x7fffffu);  // 23 mantissa bits kept
+    const uint32_t rest = (uint32_t)(u & 0x1fffffffu);       // 29 bits dropped
+    uint32_t bits = ((uint32_t)fe << 23) | top;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (top & 1u))) bits += 1u;  // a carry bumps the exponent
+    return __uint_as_float(sign | bits);
+}
+
+__device__ __forceinline__ double f2d_bits(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 255u) return (double)f;
+    const uint64_t u = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e - 127u + 1023u) << 52) |
+                       ((uint64_t)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)u);
+}
+
 __host__ __device__ __forceinline__ df df_from_double(double x) {
+#ifdef __CUDA_ARCH__
+    const float h = d2f_rn_bits(x);
+    return df{h, d2f_rn_bits(x - f2d_bits(h))};
+#else
     const float h = (float)x;
     const float l = (float)(x - (double)h);
     return df{h, l};
+#endif
 }
 
-__host__ __device__ __forceinline__ double df_to_double(df a) { return (double)a.h + (double)a.l; }
+__host__ __device__ __forceinline__ double df_to_double(df a) {
+#ifdef __CUDA_ARCH__
+    return f2d_bits(a.h) + f2d_bits(a.l);
+#else
+    return (double)a.h + (double)a.l;
+#endif
+}
 
 // ---- amplitude accessors: register-wide kernels are written once for every storage format ------
 // Storage is 16 bytes per amplitude for F64 and DF64, 8 bytes (complex<f32>) for C32; the pointer
@@ -153,7 +189,7 @@ struct AccF64 {
 struct AccDF64 {
     static __device__ __forceinline__ double2 load(const double2* p, uint64_t i) {
         const float4 v = reinterpret_cast<const float4*>(p)[i];
-        return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+        return make_double2(df_to_double(df{v.x, v.y}), df_to_double(df{v.z, v.w}));
     }
     static __device__ __forceinline__ void store(double2* p, uint64_t i, double2 v) {
         const df r = df_from_double(v.x), m = df_from_double(v.y);

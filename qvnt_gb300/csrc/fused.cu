@@ -691,7 +691,7 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
 }
 
 __device__ __forceinline__ double amp_nsq(float4 a) {
-    const double re = (double)a.x + (double)a.y, im = (double)a.z + (double)a.w;
+    const double re = df_to_double(df{a.x, a.y}), im = df_to_double(df{a.z, a.w});
     return re * re + im * im;
 }
 

@@ -338,3 +338,27 @@ def test_full_size_round_trip_30q():
     a0 = q.amplitudes_range(0, 1)[0]
     assert abs(a0 - 1.0) < 1e-10
     assert abs(q.get_absolute() - 1.0) < 1e-11
+
+
+def test_double_float_storage_conversion_exact():
+    """The device's f64 <-> double-float conversion (bit operations) equals the IEEE conversions:
+    hi = float(x), lo = float(x - hi), back = hi + lo, for ordinary values, ties, zeros, float
+    subnormals and values beyond the float range."""
+    rng = np.random.default_rng(12)
+    n = 12
+    x = rng.normal(size=2 << n) * np.exp(rng.uniform(-80, 80, size=2 << n))
+    f = rng.normal(size=64).astype(np.float32).astype(np.float64)
+    ulp = np.spacing(f.astype(np.float32)).astype(np.float64)
+    special = np.concatenate([f + ulp / 2, f - ulp / 2, f + ulp * 1.5, [0.0, -0.0, 1e-40, -3e-39, 1e-320, 3.5e38,
+                                                                      -1e39, 1.0, -1.0, 2.0 ** -126, 2.0 ** -149]])
+    x[:special.size] = special
+    q = QReg.new(n)
+    q.set_engine(ENGINE_FUSED)
+    q.set_amplitudes(x.view(np.complex128))
+    got = q.amplitudes().view(np.float64)
+    with np.errstate(over="ignore", invalid="ignore"):
+        hi = x.astype(np.float32)
+        lo = (x - hi.astype(np.float64)).astype(np.float32)
+        want = hi.astype(np.float64) + lo.astype(np.float64)
+    fin = np.isfinite(want)
+    assert np.array_equal(got[fin], want[fin])
