@@ -547,8 +547,11 @@ def main():
             "wall_s": wall,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "peak_source": peak_src, "kernel": "fused_pass_kernel" if engine == ENGINE_FUSED else "plain_gate_kernel",
-                         "launches_timed": kern_n, "avg_launch_ms": avg_launch_ms},
+                         "peak_source": peak_src, "kernel": "fused_df_kernel" if engine == ENGINE_FUSED else "plain_gate_kernel",
+                         "launches_timed": kern_n, "avg_launch_ms": avg_launch_ms,
+                         "regime": "compute-bound: double-float arithmetic on the FP32/ALU pipes; achieved is one "
+                                   "pass's algorithmic bytes over its duration, and a pass carries ~18 gates "
+                                   "at the default pass budget (800)"},
             "plain_f64_gpu": plain,
             "cpu_baseline": cpu,
             "e2e": e2e,
