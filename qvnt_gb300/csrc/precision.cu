@@ -7,9 +7,8 @@
 // gates only when their supports are disjoint), multiplying their matrices in double precision.
 // Blocks are grouped into PASSES: a pass picks 13 tile qubits (12 for a 12-qubit register): the 7
 // lowest, so a tile is a set of 1 KB runs, plus the qubits of up to kMaxPB blocks.  Each CTA,
-// persistent over tiles:
-//   1. stages the tile (8192 amplitudes, 64 KB) into shared memory with TMA bulk copies, the next
-//      tile's copies running into a second buffer while this one is processed;
+// persistent over tiles, runs two independent pipelines (warp groups), each of which:
+//   1. stages its tile (8192 amplitudes, 64 KB) into shared memory with TMA bulk copies;
 //   2. per block: threads repack the tile into the MMA operand A (2 x 128 rows = the 8 other tile
 //      bits, 64 columns = the block's 32 amplitudes as (re, im)), split into TF32 hi and lo parts and
 //      written to tensor memory with tcgen05.st; one thread issues, per 128-row half,
@@ -185,32 +184,38 @@ __device__ __forceinline__ float tf32_rna(float x) {
     return __uint_as_float(r);
 }
 
-// One pass.  A tile holds 2^k amplitudes (k = 12 or 13): 2^(k-5) operand rows in halves of 128 (the
-// MMA's M); per block and half, the TF32 hi/lo operand A is written to tensor memory with tcgen05.st
-// (lanes = rows, one column per element) next to that half's accumulator:
-//   columns   0..127  D of half 0 / 1 (64 each)
-//   columns 128..255  A_hi of half 0 / 1
-//   columns 256..383  A_lo of half 0 / 1
+// One pass.  A tile holds 2^k amplitudes (k = 13, or 12 for a 12-qubit register): 2^(k-5) operand
+// rows in halves of 128 (the MMA's M).  The 16 warps form two groups of 8, each an independent
+// pipeline over its own tiles (tile buffer, tensor-memory columns 256 g .. + 255, mbarriers, named
+// barrier 1 + g), so that one group issues while the other waits on its MMAs, copies or barriers.  Per group, tensor
+// memory holds D of both 128-row halves (columns 0..127) and one operand slot, A_hi (128..191) and
+// A_lo (192..255), that the halves take in turn: half 1 is repacked once half 0's MMAs are done, and
+// half 0 is read back while half 1's MMAs run.
+__device__ __forceinline__ void group_sync(uint32_t g) {
+    asm volatile("bar.sync %0, 256;" ::"r"(1u + g) : "memory");
+}
+
 __global__ void __launch_bounds__(kNT, 1)
     precision_tc_kernel(float2* __restrict__ psi, const float* __restrict__ wts, const __grid_constant__ PPassParams P,
-                        int* __restrict__ err) {
+                         int* __restrict__ err) {
     constexpr uint32_t kCols = 512;
     extern __shared__ __align__(1024) unsigned char smem[];
-    // two tile buffers: the next tile's load overlaps the current tile's blocks
-    float2* tiles = reinterpret_cast<float2*>(smem);
+    float2* tiles = reinterpret_cast<float2*>(smem);  // one tile buffer per group
     float* w_sm = reinterpret_cast<float*>(smem + 2 * kSmemTile);
     __shared__ uint64_t seg_off[1 << (kPT - kBQ)];
     __shared__ uint32_t mpos[kMaxPB][kMaxRows];
     __shared__ uint32_t rpos[kMaxPB][kBD];
     __shared__ __align__(8) uint64_t bar_tma[2];
-    __shared__ __align__(8) uint64_t bar_mma;
+    __shared__ __align__(8) uint64_t bar_mma[2];
     __shared__ uint32_t tmem_base;
-    __shared__ int s_abort;
+    __shared__ int s_abort[2];
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t g = warp >> 3;                  // pipeline group
+    const uint32_t gw = warp & 7u;                 // warp within the group
     const uint32_t k = P.k, c = P.c, nb = P.nblocks;
     const uint32_t nseg = 1u << (k - c);
     const uint32_t seg_amps = 1u << c;
-    const uint32_t rows = 1u << (k - kBQ);   // 128 or 256
+    const uint32_t rows = 1u << (k - kBQ);
     const uint32_t halves = rows >> 7;
     const uint32_t tile_amps = 1u << k;
 
@@ -223,7 +228,7 @@ __global__ void __launch_bounds__(kNT, 1)
     for (uint32_t b = 0; b < nb; ++b) {
         uint32_t bm = 0;
         for (int j = 0; j < kBQ; ++j) bm |= 1u << P.blocks[b].bits[j];
-        if (tid < rows) {  // the other tile bits carry the operand row m
+        if (tid < rows) {
             uint32_t pos = 0, bit = 0;
             for (uint32_t p = 0; p < k; ++p) {
                 if ((bm >> p) & 1u) continue;
@@ -247,141 +252,143 @@ __global__ void __launch_bounds__(kNT, 1)
         tmem_relinquish();
     }
     if (tid == 0) {
-        mbar_init(&bar_tma[0], 1);
-        mbar_init(&bar_tma[1], 1);
-        mbar_init(&bar_mma, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&bar_tma[i], 1);
+            mbar_init(&bar_mma[i], 1);
+            s_abort[i] = 0;
+        }
         fence_mbar_init();
-        s_abort = 0;
     }
-    __syncthreads();  // seg_off and the barriers are ready
-    // tile base index: tile number with zeros inserted at the tile qubits
-    auto tile_base = [&](uint64_t t) {
+    fence_proxy_async();  // the weights written above are read by the tensor cores
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = tmem_base + 256u * g;
+    const uint32_t lane_base = (32u * (gw & 3u)) << 16;  // this warp's lane quadrant
+    const uint32_t grp = gw >> 2;                        // column group: amplitudes 16 grp .. + 15
+    float2* tile = tiles + (size_t)g * kTileAmps;
+    const bool leader = gw == 0;                         // warp issuing the copies and the MMAs
+    uint32_t ph_tma = 0, ph_mma = 0;
+    // per half: operand repack, and read-back of the accumulator into the tile
+    auto repack = [&](uint32_t b, uint32_t h) {
+        const uint32_t m = 128u * h + 32u * (gw & 3u) + lane;
+        const uint32_t mp = mpos[b][m];
+#pragma unroll
+        for (uint32_t half = 0; half < 2; ++half) {
+            uint32_t hv[16], lv[16];
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j) {
+                const float2 x = tile[mp + rpos[b][16u * grp + 8u * half + j]];
+                const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
+                hv[2 * j] = __float_as_uint(hr);
+                hv[2 * j + 1] = __float_as_uint(hm);
+                lv[2 * j] = __float_as_uint(x.x - hr);
+                lv[2 * j + 1] = __float_as_uint(x.y - hm);
+            }
+            tmem_st16(tmem + lane_base + 128u + 32u * grp + 16u * half, hv);
+            tmem_st16(tmem + lane_base + 192u + 32u * grp + 16u * half, lv);
+        }
+        tmem_st_wait();
+    };
+    auto readback = [&](uint32_t b, uint32_t h) {
+        const uint32_t m = 128u * h + 32u * (gw & 3u) + lane;
+        const uint32_t mp = mpos[b][m];
+#pragma unroll
+        for (uint32_t half = 0; half < 2; ++half) {
+            uint32_t v[16];
+            tmem_ld16(tmem + lane_base + 64u * h + 32u * grp + 16u * half, v);
+            tmem_ld_wait();
+#pragma unroll
+            for (uint32_t j = 0; j < 8; ++j)
+                tile[mp + rpos[b][16u * grp + 8u * half + j]] =
+                    make_float2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+        }
+    };
+    auto issue = [&](uint32_t b, uint32_t h) {  // leader lane 0: the half's 24 MMAs and a commit
+        tc_after_sync();
+        const uint32_t wh = smem_addr(w_sm + (size_t)b * 2 * kWFloats), wl = wh + kWFloats * 4;
+        const uint32_t bs[3] = {wh, wl, wh};
+        const uint32_t as[3] = {tmem + 192u, tmem + 128u, tmem + 128u};  // lo, hi, hi
+        uint32_t acc = 0;
+        for (int term = 0; term < 3; ++term)
+#pragma unroll
+            for (uint32_t ks = 0; ks < 8; ++ks) {
+                mma_tf32_ta(tmem + 64u * h, as[term] + ks * 8u, smem_desc(bs[term] + ks * 256u), acc);
+                acc = 1;
+            }
+        mma_commit(&bar_mma[g]);
+    };
+    auto wait_mma = [&]() {
+        if (!mbar_wait(&bar_mma[g], ph_mma)) {
+            atomicExch(err, 1);
+            s_abort[g] = 1;
+        }
+        ph_mma ^= 1u;
+        tc_after_sync();
+    };
+    for (uint64_t t = 2ull * blockIdx.x + g; t < P.ntiles; t += 2ull * gridDim.x) {
         uint64_t base = t;
         for (uint32_t p = 0; p < k; ++p) {
             const uint32_t q = P.tq[p];
             base = ((base >> q) << (q + 1)) | (base & ((1ull << q) - 1ull));
         }
-        return base;
-    };
-    // warp 0 issues the bulk copies of one tile into buffer `buf`
-    auto load_tile = [&](uint64_t t, uint32_t buf) {
-        const uint64_t base = tile_base(t);
-        float2* tile = tiles + (size_t)buf * kTileAmps;
-        if (lane == 0) {
-            fence_proxy_async();
-            mbar_expect_tx(&bar_tma[buf], tile_amps * 8u);
+        if (leader) {
+            if (lane == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(&bar_tma[g], tile_amps * 8u);
+            }
+            __syncwarp();
+            for (uint32_t s = lane; s < nseg; s += 32)
+                bulk_load(tile + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 8u, &bar_tma[g]);
         }
-        __syncwarp();
-        for (uint32_t s = lane; s < nseg; s += 32)
-            bulk_load(tile + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 8u, &bar_tma[buf]);
-    };
-    if (warp == 0 && (uint64_t)blockIdx.x < P.ntiles) load_tile(blockIdx.x, 0);
-    fence_proxy_async();  // the weights written above are read by the tensor cores
-    tc_before_sync();
-    __syncthreads();
-    tc_after_sync();
-    const uint32_t tmem = tmem_base;
-    const uint32_t lane_base = (32u * (warp & 3u)) << 16;  // this warp's tensor-memory lane quadrant
-    const uint32_t grp = warp >> 2;                       // column group: amplitudes 8 grp .. + 7
-    uint32_t ph_tma[2] = {0, 0};
-    uint32_t ph_mma = 0;
-    uint32_t it = 0;
-    for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x, ++it) {
-        const uint32_t cur = it & 1u;
-        float2* tile = tiles + (size_t)cur * kTileAmps;
-        if (!mbar_wait(&bar_tma[cur], ph_tma[cur])) {
+        if (!mbar_wait(&bar_tma[g], ph_tma)) {
             atomicExch(err, 1);
-            s_abort = 1;
+            s_abort[g] = 1;
         }
-        ph_tma[cur] ^= 1u;
-        __syncthreads();
-        if (s_abort) break;
-        if (warp == 0 && t + gridDim.x < P.ntiles) {
-            bulk_wait_read();  // the store of the other buffer has read it
-            load_tile(t + gridDim.x, cur ^ 1u);
-        }
+        ph_tma ^= 1u;
+        group_sync(g);
+        if (s_abort[g]) break;
         for (uint32_t b = 0; b < nb; ++b) {
-            // warp w writes rows 32 (w % 4) .. + 31 of each half (its lane quadrant), columns
-            // 16 (w / 4) .. + 15 of A_hi and A_lo: amplitudes r = 8 (w / 4) .. + 7 of the row
-            for (uint32_t h = 0; h < halves; ++h) {
-                const uint32_t m = 128u * h + 32u * (warp & 3u) + lane;
-                const uint32_t mp = mpos[b][m];
-                uint32_t hv[16], lv[16];
-#pragma unroll
-                for (uint32_t j = 0; j < 8; ++j) {
-                    const float2 x = tile[mp + rpos[b][8u * grp + j]];
-                    const float hr = tf32_rna(x.x), hm = tf32_rna(x.y);
-                    hv[2 * j] = __float_as_uint(hr);
-                    hv[2 * j + 1] = __float_as_uint(hm);
-                    lv[2 * j] = __float_as_uint(x.x - hr);
-                    lv[2 * j + 1] = __float_as_uint(x.y - hm);
-                }
-                tmem_st16(tmem + lane_base + 128u + 64u * h + 16u * grp, hv);
-                tmem_st16(tmem + lane_base + 256u + 64u * h + 16u * grp, lv);
-            }
-            tmem_st_wait();
+            repack(b, 0);
             tc_before_sync();
-            __syncthreads();
-            if (tid == 0) {
-                tc_after_sync();
-                const uint32_t wh = smem_addr(w_sm + (size_t)b * 2 * kWFloats), wl = wh + kWFloats * 4;
-                const uint32_t bs[3] = {wh, wl, wh};
-                for (uint32_t h = 0; h < halves; ++h) {
-                    const uint32_t as[3] = {tmem + 256u + 64u * h, tmem + 128u + 64u * h,
-                                            tmem + 128u + 64u * h};  // lo, hi, hi
-                    uint32_t acc = 0;
-                    for (int term = 0; term < 3; ++term)
-#pragma unroll
-                        for (uint32_t ks = 0; ks < 8; ++ks) {
-                            mma_tf32_ta(tmem + 64u * h, as[term] + ks * 8u, smem_desc(bs[term] + ks * 256u), acc);
-                            acc = 1;
-                        }
-                }
-                mma_commit(&bar_mma);
-            }
-            if (!mbar_wait(&bar_mma, ph_mma)) {
-                atomicExch(err, 1);
-                s_abort = 1;
-            }
-            ph_mma ^= 1u;
-            tc_after_sync();
-            // warp w: accumulator lanes of its quadrant (rows m), columns 16 (w / 4) .. + 15
-            for (uint32_t h = 0; h < halves; ++h) {
-                uint32_t v[16];
-                tmem_ld16(tmem + lane_base + 64u * h + 16u * grp, v);
-                tmem_ld_wait();
-                const uint32_t m = 128u * h + 32u * (warp & 3u) + lane;
-                const uint32_t mp = mpos[b][m];
-#pragma unroll
-                for (uint32_t j = 0; j < 8; ++j)
-                    tile[mp + rpos[b][8u * grp + j]] = make_float2(__uint_as_float(v[2 * j]),
-                                                                   __uint_as_float(v[2 * j + 1]));
+            group_sync(g);
+            if (leader && lane == 0) issue(b, 0);
+            wait_mma();
+            if (halves == 2) {
+                repack(b, 1);  // the operand slot is free: half 0's MMAs are done
+                tc_before_sync();
+                group_sync(g);
+                if (leader && lane == 0) issue(b, 1);
+                readback(b, 0);  // while half 1's MMAs run
+                wait_mma();
+                readback(b, 1);
+            } else {
+                readback(b, 0);
             }
             tc_before_sync();
-            __syncthreads();
-            if (s_abort) break;
+            group_sync(g);
+            if (s_abort[g]) break;
         }
-        if (s_abort) break;
+        if (s_abort[g]) break;
         fence_proxy_async();
-        __syncthreads();
-        if (warp == 0) {
-            const uint64_t base = tile_base(t);
+        group_sync(g);
+        if (leader) {
             for (uint32_t s = lane; s < nseg; s += 32)
                 bulk_store(psi + (base | seg_off[s]), tile + (size_t)s * seg_amps, seg_amps * 8u);
             bulk_commit();
+            bulk_wait_read();  // the tile buffer is reused by the next load
         }
+        group_sync(g);
     }
-    if (s_abort) {
-        // copies or MMAs may still be in flight: wait on every barrier once more (bounded)
-        mbar_wait(&bar_tma[0], ph_tma[0]);
-        mbar_wait(&bar_tma[1], ph_tma[1]);
-        mbar_wait(&bar_mma, ph_mma);
+    if (s_abort[g]) {
+        mbar_wait(&bar_tma[g], ph_tma);
+        mbar_wait(&bar_mma[g], ph_mma);
     }
-    if (warp == 0) bulk_wait_all();
+    if (leader) bulk_wait_all();
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
-    if (warp == 0) tmem_dealloc(tmem, kCols);
+    if (warp == 0) tmem_dealloc(tmem_base, kCols);
 }
 
 // ---- host: dense gate matrices, blocks, passes ----------------------------------------------------
@@ -680,8 +687,8 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
             P.blocks[j].w_off = (uint32_t)(p.members[j] * 2 * kWFloats);
         }
         const size_t smem = 2 * kSmemTile + P.nblocks * kSmemW;
-        uint64_t grid = (uint64_t)r->ctx->geo.sms;
-        if (grid > P.ntiles) grid = P.ntiles;
+        // one CTA per SM, two tiles at a time (one per pipeline group)
+        const uint64_t grid = std::min<uint64_t>((uint64_t)r->ctx->geo.sms, (P.ntiles + 1) / 2);
         cudaEvent_t stop = nullptr;
         st = timing_begin(r, &stop);
         if (st) return st;
