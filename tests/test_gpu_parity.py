@@ -2,7 +2,7 @@
 
 Bar: the PLAIN engine (one pass per SingleOp, qvnt's operand order, no FMA contraction) is
 bit-identical to the oracle; the FUSED engine agrees within 1e-12 max-abs on every amplitude
-(the f64 tolerance of the benchmark spec).  Measured indices are identical given the same draw,
+(the f64 tolerance this engine is built to).  Measured indices are identical given the same draw,
 except where the draw falls within 1e-12 of a cumulative-probability boundary.
 """
 import math
