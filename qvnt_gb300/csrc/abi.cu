@@ -127,7 +127,7 @@ void reg_free(qvnt_reg* r) {
     if (!r) return;
     cudaSetDevice(r->ctx->device);
     if (r->stream) cudaStreamSynchronize(r->stream);
-    r->fused.release();
+    r->bufs.release();
     if (r->psi) cudaFree(r->psi);
     if (r->alt) cudaFree(r->alt);
     if (r->scratch) cudaFree(r->scratch);

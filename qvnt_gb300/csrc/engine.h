@@ -13,8 +13,9 @@ namespace qvnt {
 constexpr uint32_t kFusedMinK = 6;
 constexpr uint32_t kFusedMaxK = 13;
 
-// Device buffers the fused engine keeps between apply calls (pass descriptors, gate tables).
-struct FusedState {
+// Buffers an engine keeps between apply calls (the precision engine's dense-block weights: a device
+// buffer and its pinned host mirror for the upload).
+struct EngineBuffers {
     void* d_buf = nullptr;
     size_t d_bytes = 0;
     void* h_buf = nullptr;  // pinned host mirror for the upload
@@ -56,7 +57,7 @@ struct qvnt_reg {
     bool timing = false;
     bool tile_grid = false;  // one CTA per tile instead of a persistent grid (shared-GPU serving)
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
-    qvnt::FusedState fused;
+    qvnt::EngineBuffers bufs;
 };
 
 namespace qvnt {

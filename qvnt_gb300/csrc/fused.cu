@@ -1734,7 +1734,7 @@ __global__ void batch_basis_kernel(float4* __restrict__ psi, const uint64_t* __r
 
 }  // namespace
 
-void FusedState::release() {
+void EngineBuffers::release() {
     if (d_buf) cudaFree(d_buf);
     if (h_buf) cudaFreeHost(h_buf);
     d_buf = nullptr;

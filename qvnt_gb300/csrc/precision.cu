@@ -641,7 +641,7 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     if (st) return st;
     // weights of every block, uploaded once per apply call
     const size_t wfl = blocks.size() * 2 * kWFloats;
-    FusedState& fs = r->fused;
+    EngineBuffers& fs = r->bufs;
     if (fs.h_buf) QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));  // the last upload has left h_buf
     if (fs.d_bytes < wfl * 4) {
         fs.release();

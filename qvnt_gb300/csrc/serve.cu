@@ -125,7 +125,7 @@ std::deque<Request*>::iterator pick(qvnt_server* s) {
     return best;
 }
 
-int run_request(qvnt_server* s, Request* r, qvnt_reg* reg) {
+int run_request(Request* r, qvnt_reg* reg) {
     int st = QVNT_OK;
     size_t g0 = 0;
     r->results.assign(r->calls.size(), 0);
@@ -145,7 +145,6 @@ int run_request(qvnt_server* s, Request* r, qvnt_reg* reg) {
         st = qvnt_reg_get_amplitudes(reg, r->amplitudes.data());
     }
     if (!st) st = qvnt_reg_sync(reg);
-    (void)s;
     return st;
 }
 
@@ -192,7 +191,7 @@ void worker(qvnt_server* s) {
             if (!st) st = qvnt::reg_set_priority(reg, priority_for(s, r->n));
             if (!st) reg->tile_grid = true;
         }
-        if (!st) st = run_request(s, r, reg);
+        if (!st) st = run_request(r, reg);
         std::string err = st ? qvnt_last_error() : std::string();
         if (st && reg) {
             qvnt_reg_destroy(reg);  // its state is unknown: do not pool it
