@@ -163,3 +163,47 @@ def test_fused_planner_terminates_and_covers(lib_built):
     assert p30 < e30
     p20, _, _ = op.plan_info(plain_circuit(20, 20, seed=1), 20)
     assert p20 < 1610
+
+
+def test_c_program_uses_the_abi(tmp_path):
+    """The header is plain C: a C99 program includes it, links the library and drives the host-side
+    entry points (builders, names, planner) that need no GPU."""
+    import shutil
+    import subprocess
+
+    from qvnt_gb300._abi import LIB_PATH
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi_check.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include <string.h>
+#include "qvnt_gb300.h"
+int main(void) {
+    qvnt_gate g[512];
+    size_t n = 0;
+    if (qvnt_op_qft(0xFull, g, 512, &n) != QVNT_OK || n != 10) return 1;          /* 4 H + 6 CRZ */
+    qvnt_gate x;
+    if (qvnt_gate_make(QVNT_GATE_X, 0x4, 0, 0.0, NULL, &x) != QVNT_OK) return 2;
+    if (qvnt_gate_c(&x, 0x3) != QVNT_OK) return 3;
+    char name[64];
+    size_t need = 0;
+    if (qvnt_gate_name(&x, name, sizeof name, &need) != QVNT_OK || strcmp(name, "C3_X4") != 0) return 4;
+    if (qvnt_gate_make(QVNT_GATE_RX, 0x3, 0, 1.0, NULL, &x) != QVNT_ERR_BAD_MASK) return 5;
+    uint64_t passes = 0, stages = 0, eg = 0;
+    if (qvnt_plan_info(g, n, 4, 0, &passes, &stages, &eg) != QVNT_OK || passes == 0) return 6;
+    printf("%s %zu %llu\n", name, n, (unsigned long long)passes);
+    return 0;
+}
+""")
+    exe = tmp_path / "abi_check"
+    inc = os.path.join(ROOT, "include")
+    libdir = os.path.dirname(LIB_PATH)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", inc, str(src), "-o", str(exe), "-L", libdir,
+                        "-lqvnt_gb300", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
+    assert run.stdout.startswith("C3_X4 10 ")
