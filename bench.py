@@ -540,6 +540,9 @@ def main():
             "config": {"workload": "random circuit %dq f64, depth %d + qft, %d gates" % (n, args.depth, ngates),
                        "n_qubits": n, "depth": args.depth, "gates": ngates, "engine": args.engine,
                        "fused_passes_per_step": passes_per_step,
+                       "arithmetic": "double-float (pairs of FP32 with error-free transforms, 48-bit significand) on "
+                                     "the FP32 pipes, within 1e-12 of the IEEE f64 oracle" if engine == ENGINE_FUSED
+                                     else "IEEE f64, bit-identical to the oracle",
                        "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "state %d GiB > L2 129 MB, no flush" % ((1 << n) * AMP_BYTES >> 30)},
             "hbm_gbs": hbm_gbs,
