@@ -235,6 +235,35 @@ int qvnt_ops_dgr(qvnt_gate* gates, size_t count);
 /* `MultiOp::c` (multi/mod.rs:125-132): controls every gate; fails if c_mask overlaps act_on. */
 int qvnt_ops_c(qvnt_gate* gates, size_t count, uint64_t c_mask);
 
+/* ---------------------------------------------------------------------------------------------
+ * Wire formats for gate lists (host only, no device work).
+ *
+ * Text: `MultiOp`'s `{:?}` (src/operator/multi/mod.rs:90-94), a list of `SingleOp::name`s
+ * (single/mod.rs:72-78) such as "[C4_X123, RX1(1.23456), U1[[Complex { re: 1.0, im: 0.0 }, ...]]]".
+ *   qvnt_ops_name   writes that text for a gate list (at most cap bytes with the terminator;
+ *                   *needed = the full length without it).
+ *   qvnt_ops_parse  reads it back (or one bare name): `len` bytes, no terminator needed; the
+ *                   gates are built as the qvnt constructors build them (qvnt_gate_make,
+ *                   qvnt_gate_c), so masks and unitarity are checked.  At most cap gates are
+ *                   written, *count = all of them.  QVNT_ERR_BAD_ARG names the byte offset of a
+ *                   syntax error.  qvnt's names do not hold everything a gate does: S, T, iSWAP,
+ *                   sqrt(SWAP) and sqrt(iSWAP) print no dagger (parsed: not daggered); a rotation
+ *                   prints 2 arg(phase) (parsed: the gate qvnt_gate_make builds for that angle);
+ *                   U2 prints a | b (parsed: a the lower bit, b the higher); non-finite numbers are
+ *                   rejected.  The binary form below keeps every bit.
+ *
+ * Binary: a versioned, CRC-32-checked little-endian stream holding every field of each gate bit
+ * for bit, alone (gates) or with the rest of a serving request (q_num, state, submit flags and the
+ * calls of qvnt_server_submit).  Encoders write the stream only when it fits (cap >= *len) and
+ * always set *len; decoders reject a bad magic, version, type, CRC, truncation, unknown fields or
+ * trailing bytes with QVNT_ERR_BAD_ARG, write at most cap records and set the full counts (call
+ * with cap = 0 to size the buffers).  A request's APPLY calls must take exactly its gate list.
+ * ------------------------------------------------------------------------------------------- */
+int qvnt_ops_name(const qvnt_gate* gates, size_t count, char* buf, size_t cap, size_t* needed);
+int qvnt_ops_parse(const char* text, size_t len, qvnt_gate* out, size_t cap, size_t* count);
+int qvnt_wire_encode_gates(const qvnt_gate* gates, size_t count, uint8_t* buf, size_t cap, size_t* len);
+int qvnt_wire_decode_gates(const uint8_t* buf, size_t len, qvnt_gate* out, size_t cap, size_t* count);
+
 /* Plans a gate list for a q_num-qubit register on the fused engine without running it (host only,
  * no device work): the number of passes (HBM round trips), register stages and engine gates it
  * lowers to.  fusion_k as for qvnt_reg_set_fusion_width (0 = automatic). */
@@ -397,6 +426,14 @@ int qvnt_server_wait(qvnt_server* server, uint64_t id, double timeout_s, uint64_
 int qvnt_server_stats(qvnt_server* server, qvnt_server_counters* out);
 int qvnt_server_latencies(qvnt_server* server, double* out, size_t cap, size_t* count);
 int qvnt_server_queued_ages(qvnt_server* server, double* out, size_t cap, size_t* count);
+
+/* A serving request as one binary wire stream (format above qvnt_ops_name): the arguments of
+ * qvnt_server_submit except the server and the arrival time.  Host only. */
+int qvnt_wire_encode_request(uint32_t q_num, uint64_t state, int flags, const qvnt_gate* gates, size_t ngates,
+                             const qvnt_call* calls, uint32_t ncalls, uint8_t* buf, size_t cap, size_t* len);
+int qvnt_wire_decode_request(const uint8_t* buf, size_t len, uint32_t* q_num, uint64_t* state, int* flags,
+                             qvnt_gate* gates, size_t gcap, size_t* ngates, qvnt_call* calls, uint32_t ccap,
+                             uint32_t* ncalls);
 
 #ifdef __cplusplus
 }

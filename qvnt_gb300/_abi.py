@@ -124,6 +124,10 @@ _PROTOS = {
     "qvnt_op_u3": (c_int, [c_double, c_double, c_double, c_u64, P(QvntGate), c_size, P(c_size)]),
     "qvnt_ops_dgr": (c_int, [P(QvntGate), c_size]),
     "qvnt_ops_c": (c_int, [P(QvntGate), c_size, c_u64]),
+    "qvnt_ops_name": (c_int, [P(QvntGate), c_size, ctypes.c_char_p, c_size, P(c_size)]),
+    "qvnt_ops_parse": (c_int, [ctypes.c_char_p, c_size, P(QvntGate), c_size, P(c_size)]),
+    "qvnt_wire_encode_gates": (c_int, [P(QvntGate), c_size, c_void, c_size, P(c_size)]),
+    "qvnt_wire_decode_gates": (c_int, [c_void, c_size, P(QvntGate), c_size, P(c_size)]),
     "qvnt_plan_info": (c_int, [P(QvntGate), c_size, c_u32, c_u32, P(c_u64), P(c_u64), P(c_u64)]),
     "qvnt_norm_sqr_noalloc": (c_int, [c_void, c_u64, c_void, c_void]),
     "qvnt_reg_stats": (c_int, [c_void, P(c_u64), P(c_u64)]),
@@ -144,6 +148,10 @@ _PROTOS = {
     "qvnt_server_stats": (c_int, [c_void, P(ServerCounters)]),
     "qvnt_server_latencies": (c_int, [c_void, P(c_double), c_size, P(c_size)]),
     "qvnt_server_queued_ages": (c_int, [c_void, P(c_double), c_size, P(c_size)]),
+    "qvnt_wire_encode_request": (c_int, [c_u32, c_u64, c_int, P(QvntGate), c_size, P(QvntCall), c_u32, c_void,
+                                         c_size, P(c_size)]),
+    "qvnt_wire_decode_request": (c_int, [c_void, c_size, P(c_u32), P(c_u64), P(c_int), P(QvntGate), c_size,
+                                         P(c_size), P(QvntCall), c_u32, P(c_u32)]),
 }
 
 

@@ -30,6 +30,7 @@ UNITS = [
     ("serve.cu", []),
     ("precision.cu", []),
     ("builders.cpp", None),
+    ("wire.cpp", None),
 ]
 
 
