@@ -427,6 +427,41 @@ int qvnt_server_stats(qvnt_server* server, qvnt_server_counters* out);
 int qvnt_server_latencies(qvnt_server* server, double* out, size_t cap, size_t* count);
 int qvnt_server_queued_ages(qvnt_server* server, double* out, size_t cap, size_t* count);
 
+/* ---------------------------------------------------------------------------------------------
+ * QASM runner: `Sym::finish` (src/qasm/sym.rs:40-74) on a register.  A program is qvnt's
+ * interpreted `int::Op` (src/qasm/int/ext_op.rs:6-16): blocks of gates, each ending in a separator,
+ * then `trailing_gates` more gates.  Block b applies the next blocks[b].gate_count gates of `gates`
+ * and then, by blocks[b].sep:
+ *   QVNT_SEP_NOP      nothing more
+ *   QVNT_SEP_MEASURE  measure_mask(a) with the next draw of u01; the k-th set bit of a sets (or, with
+ *                     QVNT_MEASURE_XOR, xors) the k-th set bit of b in *creg from the measured bit
+ *   QVNT_SEP_IF       the block's gates run only if the bits of *creg under a (within c_num bits),
+ *                     packed low to high, equal b (`CReg::get_by_mask`, register/class.rs:115-125)
+ *   QVNT_SEP_RESET    reset_by_mask(a)
+ * *creg is the classical register (`CReg`, c_num <= 64 bits) on entry and on return; *draws_used
+ * the draws taken.  Blocks, gates (against the register) and the draws of every MEASURE block
+ * (in [0, 1)) are checked before anything runs; an invalid program changes nothing.
+ * No counterpart of the QASM parser (qvnt-qasm) is built: the caller lowers the program.
+ * ------------------------------------------------------------------------------------------- */
+#define QVNT_SEP_NOP 0u
+#define QVNT_SEP_MEASURE 1u
+#define QVNT_SEP_IF 2u
+#define QVNT_SEP_RESET 3u
+#define QVNT_MEASURE_SET 0
+#define QVNT_MEASURE_XOR 1
+
+typedef struct qvnt_block {
+    uint32_t sep;         /* QVNT_SEP_* */
+    uint32_t reserved;
+    uint64_t gate_count;  /* gates taken from the program's list */
+    uint64_t a;           /* MEASURE: qubit mask; IF: classical mask; RESET: qubit mask */
+    uint64_t b;           /* MEASURE: classical mask; IF: value */
+} qvnt_block;
+
+int qvnt_program_run(qvnt_reg* reg, uint32_t c_num, int measure_op, const qvnt_gate* gates,
+                     const qvnt_block* blocks, uint32_t nblocks, uint64_t trailing_gates, const double* u01,
+                     uint32_t nu01, uint64_t* creg, uint32_t* draws_used);
+
 /* A serving request as one binary wire stream (format above qvnt_ops_name): the arguments of
  * qvnt_server_submit except the server and the arrival time.  Host only. */
 int qvnt_wire_encode_request(uint32_t q_num, uint64_t state, int flags, const qvnt_gate* gates, size_t ngates,

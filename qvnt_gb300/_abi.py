@@ -54,6 +54,22 @@ class QvntCall(ctypes.Structure):
     ]
 
 
+SEP_NOP, SEP_MEASURE, SEP_IF, SEP_RESET = 0, 1, 2, 3
+MEASURE_SET, MEASURE_XOR = 0, 1
+
+
+class QvntBlock(ctypes.Structure):
+    """`qvnt_block`: one `(MultiOp, Sep)` block of a runner program."""
+
+    _fields_ = [
+        ("sep", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("gate_count", ctypes.c_uint64),
+        ("a", ctypes.c_uint64),
+        ("b", ctypes.c_uint64),
+    ]
+
+
 class ServerCounters(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint64) for name in ("submitted", "shed", "completed", "failed", "queued",
                                                       "running", "peak_running", "bytes_active", "bytes_pooled")] + [
@@ -148,6 +164,8 @@ _PROTOS = {
     "qvnt_server_stats": (c_int, [c_void, P(ServerCounters)]),
     "qvnt_server_latencies": (c_int, [c_void, P(c_double), c_size, P(c_size)]),
     "qvnt_server_queued_ages": (c_int, [c_void, P(c_double), c_size, P(c_size)]),
+    "qvnt_program_run": (c_int, [c_void, c_u32, c_int, P(QvntGate), P(QvntBlock), c_u32, c_u64, P(c_double), c_u32,
+                                 P(c_u64), P(c_u32)]),
     "qvnt_wire_encode_request": (c_int, [c_u32, c_u64, c_int, P(QvntGate), c_size, P(QvntCall), c_u32, c_void,
                                          c_size, P(c_size)]),
     "qvnt_wire_decode_request": (c_int, [c_void, c_size, P(c_u32), P(c_u64), P(c_int), P(QvntGate), c_size,

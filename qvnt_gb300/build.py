@@ -31,6 +31,7 @@ UNITS = [
     ("precision.cu", []),
     ("builders.cpp", None),
     ("wire.cpp", None),
+    ("program.cpp", None),
 ]
 
 
