@@ -462,6 +462,21 @@ int qvnt_program_run(qvnt_reg* reg, uint32_t c_num, int measure_op, const qvnt_g
                      const qvnt_block* blocks, uint32_t nblocks, uint64_t trailing_gates, const double* u01,
                      uint32_t nu01, uint64_t* creg, uint32_t* draws_used);
 
+/* A program as text (host only): qvnt's `Debug` of `int::Op` (src/qasm/int/ext_op.rs:77-112), what
+ * `Int::get_ops_tree` returns (src/qasm/int/mod.rs:398-400), e.g.
+ * "[H3, H4] -> Measure(11 => 11) -> if c[1] == 1 { [X4] } -> [Z4]" (masks in binary).
+ *   qvnt_program_format  writes it (at most cap bytes with the terminator; *needed = full length).
+ *   qvnt_program_parse   reads it back; gate names as qvnt_ops_parse reads them.  Two gate lists in
+ *                        a row make a NOP block; a list before Measure/Reset is that block's gates.
+ *                        At most gcap gates and bcap blocks are written, the counts are always set.
+ * The text does not show an empty NOP block or where a NOP block ends and the next block's gates
+ * begin, so a parsed program may group its gates differently; it runs the same gates in the same
+ * order with the same separators, and formats to the same text. */
+int qvnt_program_format(const qvnt_gate* gates, const qvnt_block* blocks, uint32_t nblocks, uint64_t trailing_gates,
+                        char* buf, size_t cap, size_t* needed);
+int qvnt_program_parse(const char* text, size_t len, qvnt_gate* gates, size_t gcap, size_t* ngates,
+                       qvnt_block* blocks, uint32_t bcap, uint32_t* nblocks, uint64_t* trailing_gates);
+
 /* A serving request as one binary wire stream (format above qvnt_ops_name): the arguments of
  * qvnt_server_submit except the server and the arrival time.  Host only. */
 int qvnt_wire_encode_request(uint32_t q_num, uint64_t state, int flags, const qvnt_gate* gates, size_t ngates,

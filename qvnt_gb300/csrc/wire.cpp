@@ -408,6 +408,54 @@ bool parse_one(Text& t, qvnt_gate* g) {
     return true;
 }
 
+// `[name, name, ...]` (the MultiOp `{:?}` list) into out.
+bool parse_list(Text& t, std::vector<qvnt_gate>& out) {
+    if (!t.expect("[")) return false;
+    t.ws();
+    if (t.eat("]")) return true;
+    for (;;) {
+        qvnt_gate g;
+        if (!parse_one(t, &g)) return false;
+        out.push_back(g);
+        t.ws();
+        if (t.eat("]")) return true;
+        if (!t.expect(",")) return false;
+    }
+}
+
+// Rust `{:b}` of a usize: binary digits, no prefix.
+bool binary(Text& t, uint64_t* v) {
+    t.ws();
+    const size_t start = t.at;
+    uint64_t x = 0;
+    while (t.at < t.n && (t.s[t.at] == '0' || t.s[t.at] == '1')) {
+        if (t.at - start >= 64) return t.error("binary number longer than 64 bits");
+        x = (x << 1) | (uint64_t)(t.s[t.at] - '0');
+        ++t.at;
+    }
+    if (t.at == start) return t.error("expected a binary number");
+    *v = x;
+    return true;
+}
+
+std::string binary_string(uint64_t v) {
+    if (!v) return "0";
+    std::string s;
+    for (; v; v >>= 1) s.insert(s.begin(), (char)('0' + (v & 1)));
+    return s;
+}
+
+int list_name(const qvnt_gate* g, size_t n, std::string* out) {
+    size_t need = 0;
+    int st = qvnt_ops_name(g, n, nullptr, 0, &need);
+    if (st) return st;
+    std::vector<char> buf(need + 1);
+    st = qvnt_ops_name(g, n, buf.data(), buf.size(), &need);
+    if (st) return st;
+    out->assign(buf.data(), need);
+    return QVNT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -419,19 +467,12 @@ int qvnt_ops_parse(const char* text, size_t len, qvnt_gate* out, size_t cap, siz
     size_t n = 0;
     bool ok = true;
     t.ws();
-    if (t.eat("[")) {
-        t.ws();
-        if (!t.eat("]")) {
-            for (;;) {
-                qvnt_gate g;
-                if (!(ok = parse_one(t, &g))) break;
-                if (out && n < cap) out[n] = g;
-                ++n;
-                t.ws();
-                if (t.eat("]")) break;
-                if (!(ok = t.expect(","))) break;
-            }
-        }
+    if (t.peek("[")) {
+        std::vector<qvnt_gate> list;
+        ok = parse_list(t, list);
+        for (size_t i = 0; ok && i < list.size(); ++i)
+            if (out && i < cap) out[i] = list[i];
+        n = list.size();
     } else {
         qvnt_gate g;
         if ((ok = parse_one(t, &g))) {
@@ -580,6 +621,111 @@ int qvnt_wire_decode_request(const uint8_t* buf, size_t len, uint32_t* q_num, ui
     *flags = (int)fl;
     *ngates = (size_t)ng;
     *ncalls = (uint32_t)nc;
+    return QVNT_OK;
+}
+
+// qvnt's `Debug` of the interpreted program, `int::Op` (src/qasm/int/ext_op.rs:77-112), which
+// `Int::get_ops_tree` returns (src/qasm/int/mod.rs:398-400): "[H1] -> Measure(1 => 1) -> if c[1] ==
+// 1 { [X2] } -> [Z2]".
+int qvnt_program_format(const qvnt_gate* gates, const qvnt_block* blocks, uint32_t nblocks, uint64_t trailing_gates,
+                        char* buf, size_t cap, size_t* needed) {
+    if (nblocks && !blocks) return set_error(QVNT_ERR_BAD_ARG, "null block list");
+    uint64_t ng = trailing_gates;
+    for (uint32_t b = 0; b < nblocks; ++b) {
+        if (blocks[b].sep > QVNT_SEP_RESET) return set_error(QVNT_ERR_BAD_ARG, "block %u: unknown separator %u", b, blocks[b].sep);
+        ng += blocks[b].gate_count;
+    }
+    if (ng && !gates) return set_error(QVNT_ERR_BAD_ARG, "null gate list");
+    std::string s, ops;
+    uint64_t g0 = 0;
+    int st;
+    for (uint32_t b = 0; b < nblocks; ++b) {
+        const qvnt_block& k = blocks[b];
+        if ((st = list_name(gates + g0, (size_t)k.gate_count, &ops))) return st;
+        g0 += k.gate_count;
+        // the first block prints its list even when empty (`{:?}`); later ones via `fmt_op`
+        const std::string shown = (b == 0 || k.gate_count) ? (b == 0 ? ops : " -> " + ops) : "";
+        switch (k.sep) {
+        case QVNT_SEP_NOP: s += shown; break;
+        case QVNT_SEP_MEASURE: s += shown + " -> Measure(" + binary_string(k.a) + " => " + binary_string(k.b) + ")"; break;
+        case QVNT_SEP_IF: s += " -> if c[" + binary_string(k.a) + "] == " + binary_string(k.b) + " { " + ops + " }"; break;
+        default: s += shown + " -> Reset(" + binary_string(k.a) + ")"; break;
+        }
+    }
+    if ((st = list_name(gates + g0, (size_t)trailing_gates, &ops))) return st;
+    if (!nblocks) s = ops;
+    else if (trailing_gates) s += " -> " + ops;
+    if (needed) *needed = s.size();
+    if (buf && cap) {
+        const size_t k = s.size() < cap - 1 ? s.size() : cap - 1;
+        memcpy(buf, s.data(), k);
+        buf[k] = 0;
+    }
+    return QVNT_OK;
+}
+
+int qvnt_program_parse(const char* text, size_t len, qvnt_gate* gates, size_t gcap, size_t* ngates, qvnt_block* blocks,
+                       uint32_t bcap, uint32_t* nblocks, uint64_t* trailing_gates) {
+    if (!ngates || !nblocks || !trailing_gates) return set_error(QVNT_ERR_BAD_ARG, "null count pointer");
+    if (!text && len) return set_error(QVNT_ERR_BAD_ARG, "null text");
+    Text t{text, len};
+    std::vector<qvnt_gate> all, pending;
+    std::vector<qvnt_block> out;
+    bool have_pending = false, ok = true;
+    auto close = [&](uint32_t sep, uint64_t a, uint64_t b) {
+        qvnt_block k;
+        memset(&k, 0, sizeof k);
+        k.sep = sep;
+        k.gate_count = pending.size();
+        k.a = a;
+        k.b = b;
+        all.insert(all.end(), pending.begin(), pending.end());
+        out.push_back(k);
+        pending.clear();
+        have_pending = false;
+    };
+    bool first = true;
+    for (;;) {
+        t.ws();
+        if (t.at == t.n) break;
+        if (!first && !(ok = t.eat("->") || t.error("expected '->'"))) break;
+        if (first) t.eat("->");  // an IF block first prints " -> if ..."
+        first = false;
+        t.ws();
+        if (t.peek("[")) {
+            if (have_pending) close(QVNT_SEP_NOP, 0, 0);  // two lists in a row: the first was a Nop block
+            if (!(ok = parse_list(t, pending))) break;
+            have_pending = true;
+        } else if (t.eat("Measure(")) {
+            uint64_t q = 0, c = 0;
+            if (!(ok = binary(t, &q) && t.expect("=>") && binary(t, &c) && t.expect(")"))) break;
+            close(QVNT_SEP_MEASURE, q, c);
+        } else if (t.eat("Reset(")) {
+            uint64_t q = 0;
+            if (!(ok = binary(t, &q) && t.expect(")"))) break;
+            close(QVNT_SEP_RESET, q, 0);
+        } else if (t.eat("if")) {
+            uint64_t c = 0, v = 0;
+            if (!(ok = t.expect("c") && t.expect("[") && binary(t, &c) && t.expect("]") && t.expect("==") &&
+                       binary(t, &v) && t.expect("{")))
+                break;
+            if (have_pending) close(QVNT_SEP_NOP, 0, 0);
+            if (!(ok = parse_list(t, pending) && t.expect("}"))) break;
+            close(QVNT_SEP_IF, c, v);
+        } else {
+            ok = t.error("expected a gate list, Measure, Reset or if");
+            break;
+        }
+    }
+    if (!ok) return set_error(QVNT_ERR_BAD_ARG, "program text: %s at byte %zu", t.why, t.why_at);
+    if (out.size() > 0xFFFFFFFFull) return set_error(QVNT_ERR_BAD_ARG, "too many blocks");
+    const uint64_t tail = pending.size();
+    all.insert(all.end(), pending.begin(), pending.end());
+    for (size_t i = 0; gates && i < all.size() && i < gcap; ++i) gates[i] = all[i];
+    for (size_t i = 0; blocks && i < out.size() && i < bcap; ++i) blocks[i] = out[i];
+    *ngates = all.size();
+    *nblocks = (uint32_t)out.size();
+    *trailing_gates = tail;
     return QVNT_OK;
 }
 

@@ -106,8 +106,46 @@ class Program:
         gates += tail
         return gate_array(gates), len(gates), blocks, len(self.blocks), len(tail)
 
+    def ops_tree(self):
+        """qvnt's `Debug` of `int::Op` (ext_op.rs:77-112), `Int::get_ops_tree`'s text."""
+        garr, _, barr, nb, tail = self.lower()
+        need = ctypes.c_size_t()
+        check(lib().qvnt_program_format(garr, barr, nb, tail, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value + 1)
+        check(lib().qvnt_program_format(garr, barr, nb, tail, buf, need.value + 1, ctypes.byref(need)))
+        return buf.value.decode()
+
+    @staticmethod
+    def parse(text):
+        """The program of an ops-tree text (qvnt_program_parse)."""
+        raw = text.encode() if isinstance(text, str) else bytes(text)
+        ng, nb, tail = ctypes.c_size_t(), ctypes.c_uint32(), ctypes.c_uint64()
+        check(lib().qvnt_program_parse(raw, len(raw), None, 0, ctypes.byref(ng), None, 0, ctypes.byref(nb),
+                                       ctypes.byref(tail)))
+        garr = (_abi.QvntGate * max(ng.value, 1))()
+        barr = (QvntBlock * max(nb.value, 1))()
+        check(lib().qvnt_program_parse(raw, len(raw), garr, ng.value, ctypes.byref(ng), barr, nb.value,
+                                       ctypes.byref(nb), ctypes.byref(tail)))
+        names = {v: k for k, v in _SEP_CODE.items()}
+        ops = [SingleOp(_copy(garr[i])) for i in range(ng.value)]
+        p, g0 = Program(), 0
+        for i in range(nb.value):
+            k = barr[i]
+            name = names[k.sep]
+            sep = {"nop": NOP, "measure": ("measure", k.a, k.b), "if": ("if", k.a, k.b), "reset": ("reset", k.a)}[name]
+            p.blocks.append((MultiOp(ops[g0:g0 + k.gate_count]), sep))
+            g0 += k.gate_count
+        p.last = MultiOp(ops[g0:])
+        return p
+
     def __repr__(self):
-        return "Program(%r, %r)" % (self.blocks, self.last)
+        return self.ops_tree()
+
+
+def _copy(g):
+    out = _abi.QvntGate()
+    ctypes.memmove(ctypes.byref(out), ctypes.byref(g), ctypes.sizeof(_abi.QvntGate))
+    return out
 
 
 def run_program(reg, program, c_num, creg_value=0, draws=None, measure_op="set"):

@@ -17,7 +17,7 @@ import pytest
 
 import oracle_ref as orc
 from qvnt_gb300 import _abi, op
-from qvnt_gb300._abi import QvntError
+from qvnt_gb300._abi import KIND, QvntError
 from qvnt_gb300.circuits import SplitMix64
 from qvnt_gb300.operator import MultiOp
 from qvnt_gb300.qasm import NOP, Program, run_program
@@ -92,7 +92,7 @@ def sym_finish_ref(n, c_num, program, state, creg, draws, measure_op):
     return psi, c.get(), d
 
 
-def random_program(n, c_num, statements, seed):
+def random_program(n, c_num, statements, seed, circuit=all_kinds_circuit):
     """Seeded programs built statement by statement, as qvnt's interpreter builds them."""
     rng = SplitMix64(seed)
     p = Program()
@@ -100,7 +100,7 @@ def random_program(n, c_num, statements, seed):
     for s in range(statements):
         k = rng.below(10)
         if k < 4:
-            p.apply(all_kinds_circuit(max(n, 3), 1 + rng.below(5), seed * 1000 + s))
+            p.apply(circuit(max(n, 3), 1 + rng.below(5), seed * 1000 + s))
         elif k < 6:
             w = 1 + rng.below(min(n, c_num))
             qs = sorted(rng.below(n) for _ in range(w))
@@ -119,9 +119,9 @@ def random_program(n, c_num, statements, seed):
             cm = (rng.next_u64() & ((1 << (c_num + 1)) - 1)) or 1  # may name a bit beyond c_num
             width = bin(cm & ((1 << c_num) - 1)).count("1")
             v = rng.below(1 << width) if rng.below(5) else (1 << width)  # sometimes never equal
-            p.if_branch(cm, v, all_kinds_circuit(max(n, 3), 1 + rng.below(2), seed * 1000 + s + 500))
+            p.if_branch(cm, v, circuit(max(n, 3), 1 + rng.below(2), seed * 1000 + s + 500))
     if rng.below(2):
-        p.apply(all_kinds_circuit(max(n, 3), 3, seed * 7 + 1))
+        p.apply(circuit(max(n, 3), 3, seed * 7 + 1))
     return p, nmeas
 
 
@@ -238,3 +238,73 @@ def test_python_entry_marshals_to_the_library(lib_built):
     with pytest.raises(QvntError) as e:
         run_program(None, p, 2, 0, [0.25])
     assert e.value.status == _abi.ERR_BAD_HANDLE
+
+
+# ------------------------------------------------------------------------------ ops-tree text
+
+def test_ops_tree_format():
+    """qvnt's `Debug` of `int::Op` (ext_op.rs:77-112): the first block prints its list with `{:?}`,
+    later empty lists print nothing, an IF block always starts with " -> ", masks print in binary."""
+    x6, h7, z2, y3 = op.x(0b110), op.h(0b111), op.z(0b010), op.y(0b011)
+    dummy = Program([(x6, NOP), (h7 * z2, ("measure", 0, 0))], y3)  # ext_op.rs:120-129
+    assert dummy.ops_tree() == "[X6] -> [H3, H4, Z2] -> Measure(0 => 0) -> [Y3]"
+    assert Program().ops_tree() == "[]"
+    assert Program(last=x6).ops_tree() == "[X6]"
+    assert Program().if_branch(0b1, 0, op.x(4)).ops_tree() == " -> if c[1] == 0 { [X4] }"
+    p = Program().measure(0b11, 0b110).reset(0b101)
+    assert p.ops_tree() == "[] -> Measure(11 => 110) -> Reset(101)"
+    p = Program().apply(h7).measure(0b11, 0b11).if_branch(0b10, 0b1, x6).apply(z2)
+    assert p.ops_tree() == "[H3, H4] -> Measure(11 => 11) -> if c[10] == 1 { [X6] } -> [Z2]"
+    assert repr(p) == p.ops_tree()
+
+
+LOSSY_IN_NAMES = {KIND["S"], KIND["T"], KIND["ISWAP"], KIND["SQRT_SWAP"], KIND["SQRT_ISWAP"]}
+ROTATION_KINDS = {KIND[k] for k in ("RX", "RY", "RZ", "RXX", "RYY", "RZZ")}
+
+
+def name_safe_circuit(rotations):
+    """all_kinds_circuit without the gates whose names lose a field (daggered S/T/iSWAP/sqrt gates,
+    a U2 whose a bit is the higher one) and, optionally, without rotations."""
+    def make(n, count, seed):
+        keep = []
+        for s in all_kinds_circuit(n, count, seed):
+            g = s.g
+            if (g.dagger and g.kind in LOSSY_IN_NAMES) or (g.kind == KIND["U2"] and g.a_mask > g.b_mask):
+                continue
+            if not rotations and g.kind in ROTATION_KINDS:
+                continue
+            keep.append(s)
+        return MultiOp(keep)
+    return make
+
+
+def test_ops_tree_text_is_a_fixed_point():
+    for seed in range(1, 31):
+        p, _ = random_program(3 + seed % 6, 1 + seed % 5, 15, seed, name_safe_circuit(False))
+        text = p.ops_tree()
+        assert Program.parse(text).ops_tree() == text, seed
+
+
+def test_ops_tree_parse_runs_the_same(harness):
+    for seed in range(1, 31):
+        n, c_num = 3 + seed % 6, 1 + seed % 5
+        p, nmeas = random_program(n, c_num, 15, seed, name_safe_circuit(True))
+        q = Program.parse(p.ops_tree())
+        assert [s for _, s in q.blocks if s != NOP] == [s for _, s in p.blocks if s != NOP]
+        rng = SplitMix64(seed)
+        draws = [rng.uniform() for _ in range(nmeas)]
+        st, used, c, psi = run_harness(harness, n, c_num, p, 1, 0, draws)
+        st2, used2, c2, psi2 = run_harness(harness, n, c_num, q, 1, 0, draws)
+        assert (st, used, c) == (st2, used2, c2) == (0, nmeas, c)
+        assert np.max(np.abs(psi - psi2)) <= 1e-12, seed  # rotations come back within an ulp or two
+
+
+@pytest.mark.parametrize("text", [
+    "[X1] Measure(1 => 1)", "[X1] -> Measure(2 => 1)", "[X1] -> Measure(1 => )", "[X1] -> Reset()",
+    "-> if c[1] == 1 [X1]", " -> if c[1] == 1 { [X1] ", "[X1] -> ", "[X1] -> Q",
+    "[X1] -> Measure(" + "1" * 65 + " => 1)", "[X1, ] -> [X2]",
+])
+def test_ops_tree_rejects(text, lib_built):
+    with pytest.raises(QvntError) as e:
+        Program.parse(text)
+    assert e.value.status == _abi.ERR_BAD_ARG
