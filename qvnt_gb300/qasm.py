@@ -3,7 +3,9 @@
 A program is qvnt's interpreted form ``int::Op`` (src/qasm/int/ext_op.rs:6-16): ``(MultiOp, Sep)``
 blocks and a trailing MultiOp.  ``Program`` builds it the way qvnt's interpreter does statement by
 statement (``apply``, ``measure``, ``reset``, ``if_branch``; src/qasm/int/mod.rs:207-305, 374-384),
-and ``Sym`` runs it on a device register with one ``qvnt_program_run`` call per ``finish``.  The
+including its quirk: an ``if`` right after unitary gates joins their NOP block unconditionally
+(``branch(Nop)`` then ``push`` merges into that block, and the IF separator is then dropped), and
+``Sym`` runs it on a device register with one ``qvnt_program_run`` call per ``finish``.  The
 OpenQASM text parser (qvnt's ``Ast``/``Int`` front end, from the qvnt-qasm crate) is not part of this
 package: the caller builds the program.
 
@@ -69,23 +71,41 @@ class Program:
     def __mul__(self, other):
         return Program(self.blocks, self.last).append(Program(other.blocks, other.last))
 
-    # One statement each, as the interpreter lowers it into a fresh program and appends it.
+    def _branch(self, sep):
+        """int/mod.rs:374-379: the pending gates become a block, if there are any."""
+        if len(self.last):
+            self.blocks.append((self.last, sep))
+            self.last = MultiOp()
+
+    def _branch_with_id(self, sep):
+        """int/mod.rs:381-384: the pending gates, even none, become a block."""
+        self.blocks.append((self.last, sep))
+        self.last = MultiOp()
+
+    # One statement each, on the program being built, as the interpreter processes them.
     def apply(self, op):
-        return self.append(Program(last=op))
+        """A gate statement (int/mod.rs:233-260): `push`."""
+        return self.push(op)
 
     def measure(self, q_mask, c_mask):
         """`measure q -> c` (int/mod.rs:213-231): bit counts must match."""
         if bin(q_mask).count("1") != bin(c_mask).count("1"):
             raise ValueError("measure: %d qubits into %d bits" % (bin(q_mask).count("1"), bin(c_mask).count("1")))
-        return self.append(Program([(MultiOp(), ("measure", q_mask, c_mask))]))
+        self._branch_with_id(("measure", q_mask, c_mask))
+        return self
 
     def reset(self, q_mask):
         """`reset q` (int/mod.rs:207-211)."""
-        return self.append(Program([(MultiOp(), ("reset", q_mask))]))
+        self._branch_with_id(("reset", q_mask))
+        return self
 
     def if_branch(self, c_mask, value, op):
-        """`if (c == value) gate` (int/mod.rs:286-305)."""
-        return self.append(Program([(_multi(op), ("if", c_mask, value))]))
+        """`if (c == value) gate` (int/mod.rs:286-305): branch(Nop), push the gate, branch(If).
+        After unitary gates the push joins their NOP block and the gate runs unconditionally."""
+        self._branch(NOP)
+        self.push(op)
+        self._branch(("if", c_mask, value))
+        return self
 
     def measure_count(self):
         return sum(1 for _, sep in self.blocks if sep[0] == "measure")

@@ -137,15 +137,28 @@ def test_builder_matches_reference_append():
 
 
 def test_builder_statements():
-    """The interpreter's lowering: measure/reset close the pending gates into a Nop block and add an
-    empty block with the separator (int/mod.rs:207-231, 381-384); an if-gate is its own block
-    (int/mod.rs:286-305); gates after a Nop block join it (ext_op.rs:40-50)."""
+    """The interpreter's lowering on one program (int/mod.rs:207-305, 374-384): measure and reset
+    close the pending gates, even none, into their block; an if after a separator is its own block."""
     p = Program().apply(op.h(0b11)).apply(op.x(1)).measure(0b11, 0b11)
-    assert p.blocks == [(op.h(0b11) * op.x(1), NOP), (MultiOp(), ("measure", 3, 3))] and len(p.last) == 0
+    assert p.blocks == [(op.h(0b11) * op.x(1), ("measure", 3, 3))] and len(p.last) == 0
     p.if_branch(0b1, 1, op.z(2)).reset(0b10).apply(op.y(1))
-    assert p.blocks[2:] == [(op.z(2), ("if", 1, 1)), (MultiOp(), ("reset", 2))] and p.last == op.y(1)
+    assert p.blocks[1:] == [(op.z(2), ("if", 1, 1)), (MultiOp(), ("reset", 2))] and p.last == op.y(1)
     with pytest.raises(ValueError):
         Program().measure(0b11, 0b1)
+
+
+def test_builder_if_after_gates_quirk(harness):
+    """qvnt's interpreter: branch(Nop) turns the pending gates into a NOP block, `push` then joins the
+    if-gate to that block (ext_op.rs:40-50) and branch(If) finds nothing pending -- the gate runs
+    unconditionally.  After a separator the if keeps its condition."""
+    p = Program().apply(op.h(0b1)).if_branch(0b1, 1, op.x(0b10))
+    assert p.blocks == [(op.h(0b1) * op.x(0b10), NOP)] and len(p.last) == 0
+    st, _, _, psi = run_harness(harness, 3, 1, p, creg=0)
+    want = orc.new_state(3, 0)
+    orc.apply((op.h(0b1) * op.x(0b10)).gates(), want)
+    assert st == 0 and np.array_equal(psi, want)
+    p = Program().apply(op.h(0b1)).measure(0b1, 0b1).if_branch(0b1, 1, op.x(0b10))
+    assert p.blocks[-1] == (op.x(0b10), ("if", 1, 1))
 
 
 def test_get_by_mask_and_zip_rules(harness):
