@@ -64,3 +64,29 @@ def test_sym_teleport_on_gpu():
     sym.reset()
     sym.measure(0b100, 0b10, 0.5)
     assert sym.get_class().get() == 0
+
+
+def test_qasm_program_on_gpu():
+    """An OpenQASM program through the front end (`Int`) and `Sym::new(int)` on the device."""
+    from qvnt_gb300 import ENGINE_PLAIN
+    from qvnt_gb300.circuits import SplitMix64
+    from qvnt_gb300.qasm import Int, sym_from_int
+
+    src = """OPENQASM 2.0;
+    qreg q[4]; creg c[2]; creg d[2];
+    gate prep(a, b) x { ry(a) x; rz(b/2) x; }
+    prep(1.1, 0.7) q[0]; h q[1]; cx q[1], q[2]; cx q[0], q[1]; h q[0];
+    measure q[0] -> c[0]; measure q[1] -> c[1];
+    if (c==2) x q[2]; if (c==1) z q[2]; if (c==3) y q[2];
+    h q[3]; measure q[2] -> d[0];
+    reset q[3];"""
+    i = Int.from_source(src)
+    sym = sym_from_int(i, engine=ENGINE_PLAIN)
+    for seed in range(8):
+        rng = SplitMix64(seed)
+        draws = [rng.uniform() for _ in range(i.q_ops.measure_count())]
+        sym.reset()
+        sym.finish(draws)
+        want, wc, _ = sym_finish_ref(4, 4, i.q_ops, 0, 0, draws, "set")
+        assert sym.get_class().get() == wc
+        assert np.max(np.abs(sym.amplitudes() - want)) <= TOL
