@@ -162,6 +162,9 @@ class Program:
         p.last = MultiOp(ops[g0:])
         return p
 
+    def __eq__(self, other):
+        return isinstance(other, Program) and self.blocks == other.blocks and self.last == other.last
+
     def __repr__(self):
         return self.ops_tree()
 
@@ -193,8 +196,17 @@ class Sym:
     def __init__(self, program, q_num, c_num, measure_op="set", ctx=None, engine=None):
         self.program = program
         self.m_op = measure_op
+        self.engine = engine
         self.q_reg = QReg(q_num, 0, ctx, engine)
         self.c_reg = CReg.new(c_num)
+
+    def init(self, int_):
+        """sym.rs:25-33: a new machine only when the program or the register sizes changed."""
+        if (self.m_op != int_.m_op or self.program != int_.q_ops or self.q_reg.num() != len(int_.q_reg)
+                or self.c_reg.num() != len(int_.c_reg)):
+            ctx, self.q_reg = self.q_reg.ctx, None
+            self.__init__(int_.q_ops, len(int_.q_reg), len(int_.c_reg), int_.m_op, ctx, self.engine)
+        return self
 
     def reset(self):
         """sym.rs:35-38"""
@@ -686,7 +698,16 @@ class Int:
         return self
 
     def get_ops_tree(self):
+        """mod.rs:398-400"""
         return self.q_ops.ops_tree()
+
+    def get_q_alias(self):
+        """mod.rs:402-404: `{:?}` of the qubit aliases, one per qubit."""
+        return "[" + ", ".join('"%s"' % a for a in self.q_reg) + "]"
+
+    def get_c_alias(self):
+        """mod.rs:406-408"""
+        return "[" + ", ".join('"%s"' % a for a in self.c_reg) + "]"
 
     def add_ast(self, ast):
         for node in ast.nodes:

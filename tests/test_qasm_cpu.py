@@ -73,6 +73,8 @@ def test_ast_gate_definition():
 
 def test_int_registers():
     i = Int.from_source("OPENQASM 2.0; qreg a[1]; qreg b[2]; creg c[3]; creg e[4];")
+    assert i.get_q_alias() == '["a", "b", "b"]' and i.get_c_alias() == '["c", "c", "c", "e", "e", "e", "e"]'
+    assert Int.from_source("qreg a[1]; h a;").q_ops == Int.from_source("qreg b[1]; h b;").q_ops
     assert i.get_q_idx(("a", None)) == 1 and i.get_q_idx(("b", 1)) == 4
     assert i.get_c_idx(("c", None)) == 7 and i.get_c_idx(("e", None)) == 120
     for bad in (lambda: i.get_q_idx(("b", 2)), lambda: i.get_q_idx(("c", None)), lambda: i.get_c_idx(("d", None))):
