@@ -167,7 +167,7 @@ def test_fused_planner_terminates_and_covers(lib_built):
 
 def test_c_program_uses_the_abi(tmp_path):
     """The header is plain C: a C99 program includes it, links the library and drives the host-side
-    entry points (builders, names, planner) that need no GPU."""
+    entry points (builders, names, planner, wire formats, program text) that need no GPU."""
     import shutil
     import subprocess
 
@@ -194,6 +194,28 @@ int main(void) {
     if (qvnt_gate_make(QVNT_GATE_RX, 0x3, 0, 1.0, NULL, &x) != QVNT_ERR_BAD_MASK) return 5;
     uint64_t passes = 0, stages = 0, eg = 0;
     if (qvnt_plan_info(g, n, 4, 0, &passes, &stages, &eg) != QVNT_OK || passes == 0) return 6;
+    /* wire formats: names -> gates -> binary stream -> gates -> names */
+    const char* text = "[C3_X4, H3, RZ1(0.5)]";
+    qvnt_gate p[8], back[8];
+    size_t np = 0, nb = 0, len = 0;
+    if (qvnt_ops_parse(text, strlen(text), p, 8, &np) != QVNT_OK || np != 3) return 7;
+    unsigned char buf[1024];
+    if (qvnt_wire_encode_gates(p, np, buf, sizeof buf, &len) != QVNT_OK || len > sizeof buf) return 8;
+    if (qvnt_wire_decode_gates(buf, len, back, 8, &nb) != QVNT_OK || nb != 3) return 9;
+    if (memcmp(p, back, 3 * sizeof(qvnt_gate)) != 0) return 10;
+    buf[len / 2] ^= 1;
+    if (qvnt_wire_decode_gates(buf, len, back, 8, &nb) != QVNT_ERR_BAD_ARG) return 11;
+    char names[256];
+    if (qvnt_ops_name(back, nb, names, sizeof names, &need) != QVNT_OK || strcmp(names, text) != 0) return 12;
+    /* a runner program as qvnt's ops-tree text */
+    const char* prog = "[H1] -> Measure(1 => 1) -> if c[1] == 1 { [X2] } -> [Z2]";
+    qvnt_block blk[4];
+    uint32_t nblk = 0;
+    uint64_t tail = 0;
+    if (qvnt_program_parse(prog, strlen(prog), p, 8, &np, blk, 4, &nblk, &tail) != QVNT_OK) return 13;
+    if (np != 3 || nblk != 2 || tail != 1 || blk[0].sep != QVNT_SEP_MEASURE || blk[1].sep != QVNT_SEP_IF) return 14;
+    if (qvnt_program_format(p, blk, nblk, tail, names, sizeof names, &need) != QVNT_OK || strcmp(names, prog) != 0)
+        return 15;
     printf("%s %zu %llu\n", name, n, (unsigned long long)passes);
     return 0;
 }
