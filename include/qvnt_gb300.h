@@ -472,6 +472,18 @@ int qvnt_program_run(qvnt_reg* reg, uint32_t c_num, int measure_op, const qvnt_g
  * The text does not show an empty NOP block or where a NOP block ends and the next block's gates
  * begin, so a parsed program may group its gates differently; it runs the same gates in the same
  * order with the same separators, and formats to the same text. */
+/* OpenQASM 2.0 source to a program for qvnt_program_run (host only): `Int::new(Ast::from_source(..))`
+ * (src/qasm/int/mod.rs:56-60).  Qubits and bits are allocated in declaration order (*q_num, *c_num:
+ * the register sizes `Sym::new` uses, at most 64 each); gate names map as qvnt's table does
+ * (src/qasm/int/gates.rs:86-126: a leading c/C controls by the first register, registers OR into one
+ * mask, sdg/tdg build S/T); `gate` definitions expand with their parameters; arguments are evaluated
+ * with pi, sqrt, exp, ln, abs, floor, ceil, round, atan2, max, min (src/qasm/int/parse.rs:5-25);
+ * `include` is skipped.  At most gcap gates and bcap blocks are written, the counts always set.
+ * Errors (syntax, unknown names, sizes, masks) return QVNT_ERR_BAD_ARG with the reason. */
+int qvnt_qasm_compile(const char* source, size_t len, uint32_t* q_num, uint32_t* c_num, qvnt_gate* gates,
+                      size_t gcap, size_t* ngates, qvnt_block* blocks, uint32_t bcap, uint32_t* nblocks,
+                      uint64_t* trailing_gates);
+
 int qvnt_program_format(const qvnt_gate* gates, const qvnt_block* blocks, uint32_t nblocks, uint64_t trailing_gates,
                         char* buf, size_t cap, size_t* needed);
 int qvnt_program_parse(const char* text, size_t len, qvnt_gate* gates, size_t gcap, size_t* ngates,

@@ -166,6 +166,8 @@ _PROTOS = {
     "qvnt_server_queued_ages": (c_int, [c_void, P(c_double), c_size, P(c_size)]),
     "qvnt_program_run": (c_int, [c_void, c_u32, c_int, P(QvntGate), P(QvntBlock), c_u32, c_u64, P(c_double), c_u32,
                                  P(c_u64), P(c_u32)]),
+    "qvnt_qasm_compile": (c_int, [ctypes.c_char_p, c_size, P(c_u32), P(c_u32), P(QvntGate), c_size, P(c_size),
+                                  P(QvntBlock), c_u32, P(c_u32), P(c_u64)]),
     "qvnt_program_format": (c_int, [P(QvntGate), P(QvntBlock), c_u32, c_u64, ctypes.c_char_p, c_size, P(c_size)]),
     "qvnt_program_parse": (c_int, [ctypes.c_char_p, c_size, P(QvntGate), c_size, P(c_size), P(QvntBlock), c_u32,
                                    P(c_u32), P(c_u64)]),

@@ -32,6 +32,7 @@ UNITS = [
     ("builders.cpp", None),
     ("wire.cpp", None),
     ("program.cpp", None),
+    ("qasm.cpp", None),
 ]
 
 

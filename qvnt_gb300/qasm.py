@@ -150,10 +150,14 @@ class Program:
         barr = (QvntBlock * max(nb.value, 1))()
         check(lib().qvnt_program_parse(raw, len(raw), garr, ng.value, ctypes.byref(ng), barr, nb.value,
                                        ctypes.byref(nb), ctypes.byref(tail)))
+        return Program._from_arrays(garr, ng.value, barr, nb.value)
+
+    @staticmethod
+    def _from_arrays(garr, ng, barr, nb):
         names = {v: k for k, v in _SEP_CODE.items()}
-        ops = [SingleOp(_copy(garr[i])) for i in range(ng.value)]
+        ops = [SingleOp(_copy(garr[i])) for i in range(ng)]
         p, g0 = Program(), 0
-        for i in range(nb.value):
+        for i in range(nb):
             k = barr[i]
             name = names[k.sep]
             sep = {"nop": NOP, "measure": ("measure", k.a, k.b), "if": ("if", k.a, k.b), "reset": ("reset", k.a)}[name]
@@ -272,7 +276,32 @@ def _finite_only(f):
 
 
 def _round(v):  # half away from zero, as f64::round
-    return math.copysign(math.floor(abs(v) + 0.5), v) if math.isfinite(v) else v
+    if not math.isfinite(v):
+        return v
+    r = math.floor(abs(v))
+    return math.copysign(r + 1.0 if abs(v) - r >= 0.5 else r, v)
+
+
+def _fmax(m, x):  # f64::max: a NaN operand yields the other one
+    return m if x != x else (x if m != m or x > m else m)
+
+
+def _fmin(m, x):
+    return m if x != x else (x if m != m or x < m else m)
+
+
+def _max_array(*xs):  # meval's max_array / min_array: a fold from -inf / +inf
+    m = float("-inf")
+    for x in xs:
+        m = _fmax(m, x)
+    return m
+
+
+def _min_array(*xs):
+    m = float("inf")
+    for x in xs:
+        m = _fmin(m, x)
+    return m
 
 
 def _div(a, b):
@@ -301,7 +330,7 @@ def _pow(a, b):
 
 _FUNCS = {"sqrt": (1, _sqrt), "exp": (1, _exp), "ln": (1, _ln), "abs": (1, abs),
           "floor": (1, _finite_only(math.floor)), "ceil": (1, _finite_only(math.ceil)), "round": (1, _round),
-          "atan2": (2, math.atan2), "max": (-1, max), "min": (-1, min)}
+          "atan2": (2, math.atan2), "max": (-1, _max_array), "min": (-1, _min_array)}
 
 
 def eval_expr(text, variables=()):
@@ -329,7 +358,7 @@ def eval_expr(text, variables=()):
             v = add()
             take(")")
             return v
-        if re.match(r"[\d.]", tok):
+        if re.match(r"\d|\.\d", tok):
             return float(tok)
         if re.match(r"[A-Za-z_]", tok):
             if peek() == "(":
@@ -438,8 +467,10 @@ class _Parser:
 
     def integer(self):
         t = self.peek()
-        if t is None or not t.isdigit():
+        if t is None or not re.match(r"[0-9]+$", t):
             raise QasmError("missing integer (token %d)" % self.i)
+        if len(t) > 18:
+            raise QasmError("integer too large (token %d)" % self.i)
         self.i += 1
         return int(t)
 
@@ -748,6 +779,8 @@ class Int:
             raise QasmError("register %s[%d] is too large" % (name, size))
         if name in self.q_reg or name in self.c_reg:
             raise QasmError("register %s is declared twice" % name)
+        if len(regs) + size > 64:
+            raise QasmError("more than 64 qubits or bits in all (a mask holds 64)")
         regs.extend([name] * size)
 
     def _apply(self, node):
@@ -790,9 +823,25 @@ class Int:
             self.q_ops._branch(("if", val, value))
 
 
+def compile_native(source):
+    """The library's C++ front end, ``qvnt_qasm_compile``: (Program, qubits, bits) for the same text
+    that ``Int.from_source`` reads; raises QvntError where ``Int`` raises QasmError."""
+    raw = source.encode() if isinstance(source, str) else bytes(source)
+    q, c, ng, nb, tail = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_size_t(), ctypes.c_uint32(), ctypes.c_uint64()
+    refs = (ctypes.byref(q), ctypes.byref(c))
+    check(lib().qvnt_qasm_compile(raw, len(raw), *refs, None, 0, ctypes.byref(ng), None, 0, ctypes.byref(nb),
+                                  ctypes.byref(tail)))
+    garr = (_abi.QvntGate * max(ng.value, 1))()
+    barr = (QvntBlock * max(nb.value, 1))()
+    check(lib().qvnt_qasm_compile(raw, len(raw), *refs, garr, ng.value, ctypes.byref(ng), barr, nb.value,
+                                  ctypes.byref(nb), ctypes.byref(tail)))
+    return Program._from_arrays(garr, ng.value, barr, nb.value), q.value, c.value
+
+
 def sym_from_int(int_, ctx=None, engine=None):
     """`Sym::new(int)` (sym.rs:16-23): registers sized by the program's declarations."""
     return Sym(int_.q_ops, len(int_.q_reg), len(int_.c_reg), int_.m_op, ctx, engine)
 
 
-__all__ = ["Program", "Sym", "run_program", "NOP", "Ast", "Int", "QasmError", "eval_expr", "sym_from_int"]
+__all__ = ["Program", "Sym", "run_program", "NOP", "Ast", "Int", "QasmError", "eval_expr", "sym_from_int",
+           "compile_native"]

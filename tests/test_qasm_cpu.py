@@ -83,7 +83,7 @@ def test_int_registers():
     assert Int.from_source("qreg q[5]; h q[2];").q_reg == ["q"] * 5  # no header needed
 
 
-@pytest.mark.parametrize("src", [
+REJECTED_SOURCES = [
     "h q[2];", "qreg q[2]; measure q -> c;", "qreg q[3]; qreg q[2];", "creg c[5]; creg c[1];",
     "qreg x[5]; creg x[1];", "creg x[1]; qreg x[5];", "qreg q[2]; h q[2];", "qreg q[2]; h q[3];",
     "qreg q[3]; g q[2];", "qreg q[4]; cx q[0], q;", "qreg q[4]; rx(2*a) q[0];", "qreg q[4]; rx(pi) q[0], q[2];",
@@ -92,23 +92,28 @@ def test_int_registers():
     "gate M q { h q[0]; }", "gate M(a, b, c) x, y { rx(a) x; ry(b) y; rz(c) z; }",
     "gate M(a, b) x, y, z { rx(a) x; ry(b) y; rz(c) z; }", "gate r q { r q; } qreg a[1]; r a;",
     "qreg q[2]; U(0, 0, 0) q[0];",
-])
+]
+
+
+@pytest.mark.parametrize("src", REJECTED_SOURCES)
 def test_int_rejects(src):
     with pytest.raises(QasmError):
         Int.from_source(src)
+
+
+OPERATION_TREE_SRC = """OPENQASM 2.0; qreg q[2]; creg c[2];
+    gate foo(x, y) a, b { rx(y*x) a; }
+    h q[0]; cx q[0], q[1]; foo(pi, 1) q[0], q[1];
+    measure q -> c;
+    if (c==1) h q[0]; if (c==2) h q[1]; if (c==3) h q[0], q[1];
+    measure q -> c;"""
 
 
 def test_int_operation_tree():
     """qvnt's `operation_tree` source (int/mod.rs:444-476), lowered by the interpreter's rules: the
     gates before the first measure ride in its block; each `if` after a separator is its own block;
     the last measure has an empty block."""
-    src = """OPENQASM 2.0; qreg q[2]; creg c[2];
-    gate foo(x, y) a, b { rx(y*x) a; }
-    h q[0]; cx q[0], q[1]; foo(pi, 1) q[0], q[1];
-    measure q -> c;
-    if (c==1) h q[0]; if (c==2) h q[1]; if (c==3) h q[0], q[1];
-    measure q -> c;"""
-    i = Int.from_source(src)
+    i = Int.from_source(OPERATION_TREE_SRC)
     assert [sep for _, sep in i.q_ops.blocks] == [("measure", 3, 3), ("if", 3, 1), ("if", 3, 2), ("if", 3, 3),
                                                   ("measure", 3, 3)]
     assert i.get_ops_tree() == ("[H1, C1_X2, RX1(3.141592653589793)] -> Measure(11 => 11) -> if c[11] == 1 { [H1] }"
@@ -182,3 +187,77 @@ def test_reference_examples_run(name, harness):  # noqa: F811
         i = Int.from_source(f.read())
     for seed in (1, 2):
         run_int(harness, i, seed)
+
+
+# ------------------------------------------------------------------------------ the C++ front end
+
+OWN_SOURCES = [
+    """OPENQASM 2.0; include "qelib1.inc"; qreg q[3]; creg c[2];
+    gate foo(a, b) x, y { rx(a) x; cx x, y; u1(b/2) y; }
+    h q[0]; cx q[0], q[1]; foo(pi/2, 0.5) q[1], q[2];
+    measure q[0] -> c[0]; measure q[1] -> c[1]; if (c == 1) x q[2]; reset q[0]; barrier q;""",
+    """qreg a[2]; qreg b[3]; creg m[2]; gate maj a, b, c { cx c, b; cx c, a; ccx a, b, c; }
+    maj a[0], b[0], b[1]; u3(0.1, -0.2e1, 3/4) b[2]; sdg a[1]; tdg b; cu1(pi^2 % 1) a[0], a[1];
+    rzz(max(0.1, 0.2)) a[0], b[2]; h a; if (m==3) sqrt_swap b[0], b[2]; measure a -> m; qft b;""",
+    "qreg q[1]; U(0, 0, 0) q[0];",
+    "qreg q[2]; creg c[2]; h q[0]; if (c==1) x q[1]; measure q -> c;",
+]
+
+
+def native_view(src):
+    from qvnt_gb300.qasm import compile_native
+    p, q, c = compile_native(src)
+    return q, c, [(sep, [bytes(g) for g in ops.gates()]) for ops, sep in p.blocks], [bytes(g) for g in p.last.gates()]
+
+
+def python_view(src):
+    i = Int.from_source(src)
+    return (len(i.q_reg), len(i.c_reg), [(sep, [bytes(g) for g in ops.gates()]) for ops, sep in i.q_ops.blocks],
+            [bytes(g) for g in i.q_ops.last.gates()])
+
+
+def same_outcome(src):
+    from qvnt_gb300._abi import QvntError
+    try:
+        want = python_view(src)
+    except QasmError:
+        want = "rejected"
+    try:
+        got = native_view(src)
+    except QvntError:
+        got = "rejected"
+    assert got == want, src[:200]
+    return want != "rejected"
+
+
+def test_native_front_end_matches(lib_built):
+    """qvnt_qasm_compile (C++) lowers every program exactly as the Python front end does, and rejects
+    the same ones, on this file's programs and the reference error cases."""
+    srcs = OWN_SOURCES + [OPERATION_TREE_SRC]
+    accepted = sum(same_outcome(s) for s in srcs)
+    assert accepted == len(srcs) - 1  # the U(...) program is rejected by both
+    for bad in REJECTED_SOURCES:
+        assert not same_outcome(bad)
+    if os.path.isdir(EXAMPLE_DIR):
+        for name in EXAMPLES:
+            with open(os.path.join(EXAMPLE_DIR, name + ".qasm")) as f:
+                assert same_outcome(f.read()), name
+
+
+def test_native_front_end_matches_on_mutations(lib_built):
+    rng = SplitMix64(77)
+    alpha = "qcrgx[](){};,->=0123456789.+-*/^pi hmeasurtif\n\""
+    accepted = 0
+    for k in range(2000):
+        s = list(OWN_SOURCES[k % 2])
+        for _ in range(1 + rng.below(4)):
+            i = rng.below(len(s))
+            r = rng.below(10)
+            if r < 4:
+                s[i] = alpha[rng.below(len(alpha))]
+            elif r < 7:
+                del s[i]
+            else:
+                s.insert(i, alpha[rng.below(len(alpha))])
+        accepted += same_outcome("".join(s))
+    assert accepted > 30
