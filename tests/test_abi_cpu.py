@@ -167,7 +167,7 @@ def test_fused_planner_terminates_and_covers(lib_built):
 
 def test_c_program_uses_the_abi(tmp_path):
     """The header is plain C: a C99 program includes it, links the library and drives the host-side
-    entry points (builders, names, planner, wire formats, program text) that need no GPU."""
+    entry points (builders, names, planner, wire formats, program text, QASM) that need no GPU."""
     import shutil
     import subprocess
 
@@ -216,6 +216,13 @@ int main(void) {
     if (np != 3 || nblk != 2 || tail != 1 || blk[0].sep != QVNT_SEP_MEASURE || blk[1].sep != QVNT_SEP_IF) return 14;
     if (qvnt_program_format(p, blk, nblk, tail, names, sizeof names, &need) != QVNT_OK || strcmp(names, prog) != 0)
         return 15;
+    /* OpenQASM text to a runner program */
+    const char* src = "OPENQASM 2.0; qreg q[2]; creg c[2]; h q[0]; cx q[0], q[1]; measure q -> c;";
+    uint32_t qn = 0, cn = 0;
+    if (qvnt_qasm_compile(src, strlen(src), &qn, &cn, p, 8, &np, blk, 4, &nblk, &tail) != QVNT_OK) return 16;
+    if (qn != 2 || cn != 2 || np != 2 || nblk != 1 || blk[0].sep != QVNT_SEP_MEASURE || blk[0].a != 3) return 17;
+    if (qvnt_qasm_compile("qreg q[1]; g q;", 15, &qn, &cn, p, 8, &np, blk, 4, &nblk, &tail) != QVNT_ERR_BAD_ARG)
+        return 18;
     printf("%s %zu %llu\n", name, n, (unsigned long long)passes);
     return 0;
 }
