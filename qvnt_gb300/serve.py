@@ -49,6 +49,14 @@ class Server:
             self._ncalls[rid.value] = (len(calls), q_num if keep_amplitudes else None)
         return rid.value
 
+    def submit_request(self, data, arrival=-1.0):
+        """Submits a request received as a binary wire stream (`qvnt_wire_encode_request`,
+        `wire.encode_request`); returns what `submit` returns."""
+        from .wire import decode_request
+        r = decode_request(data)
+        gates = _abi.gate_array(r["ops"].gates()) if len(r["ops"]) else None
+        return self.submit(r["q_num"], r["state"], gates, r["calls"], arrival, r["keep_amplitudes"], r["detached"])
+
     def wait(self, rid, timeout=-1.0):
         """(measured values per call, final amplitudes or None, latency in seconds)."""
         ncalls, keep_n = self._ncalls.pop(rid)

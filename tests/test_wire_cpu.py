@@ -379,3 +379,27 @@ def test_request_rejects_inconsistent_calls(lib_built):
     body = b"QVNW\x01\x02\x00\x00" + py_varint(0) + py_varint(3) + py_varint(0) + py_varint(0) + py_varint(1)
     expect_bad(wire.decode_request, with_crc(body + bytes([0]) + py_varint(5) + py_varint(0) + b"\0" * 8))
     expect_bad(wire.decode_request, with_crc(body))  # one call announced, none present
+
+
+def test_server_submit_request_glue(lib_built):
+    """Server.submit_request hands the decoded request to Server.submit unchanged (a recording
+    stand-in replaces the device submit)."""
+    from qvnt_gb300.serve import Server
+
+    class Recorder(Server):
+        def __init__(self):
+            self.seen = None
+
+        def submit(self, q_num, state, gates, calls, arrival=-1.0, keep_amplitudes=False, detached=False):
+            n = sum(c[1] for c in calls if c[0] == "apply")
+            self.seen = (q_num, state, [bytes(gates[i]) for i in range(n)] if gates is not None else None, calls,
+                         arrival, keep_amplitudes, detached)
+            return 7
+
+    ops = op.qft(0b1111) * op.x(1)
+    calls = [("apply", 5), ("measure", 0b11, 0.5), ("apply", len(ops) - 5)]
+    rec = Recorder()
+    assert rec.submit_request(wire.encode_request(4, 2, ops, calls, keep_amplitudes=True), arrival=1.5) == 7
+    assert rec.seen == (4, 2, [bytes(g) for g in ops.gates()], calls, 1.5, True, False)
+    rec.submit_request(wire.encode_request(3, 0, None, [("measure", 1, 0.25)], detached=True))
+    assert rec.seen == (3, 0, None, [("measure", 1, 0.25)], -1.0, False, True)
