@@ -137,6 +137,7 @@ def test_bits_iter_vreg_creg(golden):
     c = CReg.with_state(8, 0b10110010)
     assert c.get_by_mask(0b11110000) == 0b1011
     assert repr(CReg.with_state(4, 0b0101)) == "(0101)"
+    assert repr(CReg.with_state(8, 123)) == "(01111011)" and CReg.with_state(8, 123).get() == 123  # class.rs:39-47
     assert (CReg.with_state(2, 0b01) * CReg.with_state(2, 0b10)).get() == 0b1001
 
 
