@@ -139,6 +139,7 @@ def test_bits_iter_vreg_creg(golden):
     assert repr(CReg.with_state(4, 0b0101)) == "(0101)"
     assert repr(CReg.with_state(8, 123)) == "(01111011)" and CReg.with_state(8, 123).get() == 123  # class.rs:39-47
     assert (CReg.with_state(2, 0b01) * CReg.with_state(2, 0b10)).get() == 0b1001
+    assert CReg.with_state(4, 11) * CReg.with_state(4, 7) == CReg.with_state(8, 123)  # class.rs:24-31
 
 
 def test_circuit_sizes(lib_built):
