@@ -1,0 +1,12 @@
+//! `rx::Op` lowered to the engine's `qvnt_gate` (its stored fields, src/operator/atomic/rx.rs).
+//! A child module of the op's own, so that it reads the op's private fields.
+use super::Op;
+use crate::gpu::ffi::{qvnt_gate, KIND_RX};
+
+impl Op {
+    pub(crate) fn gb300_lower(&self, g: &mut qvnt_gate) {
+        g.kind = KIND_RX;
+        g.a_mask = self.a_mask as u64;
+        g.phase = [self.phase.re, self.phase.im];
+    }
+}
