@@ -106,8 +106,13 @@ typedef struct qvnt_reg qvnt_reg;
  *   PRECISION keeps complex<f32> amplitudes (8 B) and fuses runs of gates into dense 5-qubit blocks
  *          (32 x 32 complex) contracted on the tensor cores (TF32 split hi + lo, FP32 accumulation);
  *          norms, probabilities and measurement stay FP64.  Registers of at least 12 qubits; gates
- *          whose targets and controls span more than 5 qubits are rejected (QVNT_ERR_UNSUPPORTED). */
-enum qvnt_engine { QVNT_ENGINE_FUSED = 0, QVNT_ENGINE_PLAIN = 1, QVNT_ENGINE_PRECISION = 2 };
+ *          whose targets and controls span more than 5 qubits are rejected (QVNT_ERR_UNSUPPORTED).
+ *   TENSOR64 keeps IEEE f64 amplitudes (the PLAIN layout) and fuses runs of gates into dense 5-qubit
+ *          blocks contracted on the tensor cores with 53-bit operands split into exact fp16 digit
+ *          products (FP32 accumulation of integers below 2^23, no rounding), one f64 rounding per
+ *          block; gates spanning more than 5 qubits with their controls, and registers below 12
+ *          qubits, run on the PLAIN kernels.  Within 1e-12 of the PLAIN engine. */
+enum qvnt_engine { QVNT_ENGINE_FUSED = 0, QVNT_ENGINE_PLAIN = 1, QVNT_ENGINE_PRECISION = 2, QVNT_ENGINE_TENSOR64 = 3 };
 
 /* ---------------------------------------------------------------------------------------------
  * Status / errors
@@ -125,6 +130,10 @@ int qvnt_ctx_create(int device, qvnt_ctx** out);
 int qvnt_ctx_destroy(qvnt_ctx* ctx);
 /* Free device memory and the total in bytes, as the CUDA runtime reports them for this device. */
 int qvnt_ctx_mem_info(qvnt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
+/* Engine (enum qvnt_engine) of the registers qvnt_reg_create makes on this context and of the
+ * scratch register of qvnt_apply_host (which runs PRECISION requests on FUSED); default FUSED.
+ * No counterpart in the reference (its one CPU path has no choice to make). */
+int qvnt_ctx_set_engine(qvnt_ctx* ctx, int engine);
 
 /* ---------------------------------------------------------------------------------------------
  * Registers (QReg, src/register/quant.rs:102-150)
@@ -277,7 +286,9 @@ int qvnt_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint32_
  * where cudaMalloc/cudaFree would synchronise the device in the middle of their stream work.
  *
  * Sum of |psi_i|^2 over a state vector the caller keeps in device memory: d_psi holds len
- * interleaved (re, im) IEEE f64 amplitudes; the sum is written to the device double *d_out.  The
+ * interleaved (re, im) IEEE f64 amplitudes and must be 16-byte aligned (it is read as double2); the
+ * sum is written to the device double *d_out (8-byte aligned).  Misaligned pointers are refused with
+ * QVNT_ERR_BAD_ARG before anything is queued.  The
  * kernels are queued on `stream` (a cudaStream_t; NULL = the legacy default stream) and the call
  * returns without waiting.  It allocates nothing: its partial sums live in a file-scope device
  * array of QVNT_NOALLOC_MAX_AMPLITUDES / 4096 doubles (512 KiB) that every GPU loading the library
@@ -313,6 +324,10 @@ int qvnt_reg_overlap(const qvnt_reg* a, const qvnt_reg* b, double* fidelity, dou
  * 5-qubit blocks. */
 int qvnt_precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* passes,
                              uint64_t* blocks);
+/* Host-side plan of the TENSOR64 engine for a gate list on q_num qubits: tensor-core passes (one
+ * dense 5-qubit block each) and gates left to single PLAIN passes (no counterpart in the reference). */
+int qvnt_tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* passes,
+                            uint64_t* plain_gates);
 /* Time the fused engine spends in its dominant kernel: CUDA events recorded around every launch of
  * the fused-pass kernel on the register's stream since the last reset (enable != 0 turns
  * recording on and clears the totals).  *ms = summed event time, *launches = number of launches. */

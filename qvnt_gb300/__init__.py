@@ -17,10 +17,10 @@ import os as _os
 _os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import operator as op  # noqa: E402
-from ._abi import ENGINE_FUSED, ENGINE_PLAIN, ENGINE_PRECISION, KIND, KINDS, MaskError, QvntError, QvntGate
+from ._abi import ENGINE_FUSED, ENGINE_PLAIN, ENGINE_PRECISION, ENGINE_TENSOR64, KIND, KINDS, MaskError, QvntError, QvntGate
 from .operator import MultiOp, SingleOp
 from .register import Context, CReg, QReg, VReg, bits_iter, default_context
 
 __all__ = ["op", "QReg", "CReg", "VReg", "MultiOp", "SingleOp", "Context", "default_context", "bits_iter",
            "QvntGate", "QvntError", "MaskError", "KIND", "KINDS", "ENGINE_FUSED", "ENGINE_PLAIN",
-           "ENGINE_PRECISION"]
+           "ENGINE_PRECISION", "ENGINE_TENSOR64"]

@@ -20,6 +20,7 @@ KIND = {name: i for i, name in enumerate(KINDS)}
 ENGINE_FUSED = 0
 ENGINE_PLAIN = 1
 ENGINE_PRECISION = 2
+ENGINE_TENSOR64 = 3
 
 
 class QvntGate(ctypes.Structure):
@@ -106,6 +107,8 @@ _PROTOS = {
     "qvnt_reg_combine_with_unitary": (c_int, [c_void, c_void, P(c_double), P(c_void)]),
     "qvnt_reg_linear_composition": (c_int, [c_void, c_void, P(c_double)]),
     "qvnt_precision_plan_info": (c_int, [P(QvntGate), c_size, c_u32, P(c_u64), P(c_u64)]),
+    "qvnt_tensor64_plan_info": (c_int, [P(QvntGate), c_size, c_u32, P(c_u64), P(c_u64)]),
+    "qvnt_ctx_set_engine": (c_int, [c_void, c_int]),
     "qvnt_reg_destroy": (c_int, [c_void]),
     "qvnt_reg_clone": (c_int, [c_void, P(c_void)]),
     "qvnt_reg_num": (c_int, [c_void, P(c_u32)]),

@@ -29,6 +29,7 @@ UNITS = [
     ("measure.cu", ["--fmad=false"]),
     ("serve.cu", []),
     ("precision.cu", []),
+    ("tensor64.cu", []),
     ("builders.cpp", None),
     ("wire.cpp", None),
     ("program.cpp", None),

@@ -283,8 +283,15 @@ uint64_t reg_len_for(uint32_t q_num) {
     return q < 8 ? 8 : q;
 }
 
+bool engine_valid(int engine) {
+    return engine == QVNT_ENGINE_FUSED || engine == QVNT_ENGINE_PLAIN || engine == QVNT_ENGINE_PRECISION ||
+           engine == QVNT_ENGINE_TENSOR64;
+}
+
 int fmt_of_engine(int engine) {
-    return engine == QVNT_ENGINE_PLAIN ? FMT_F64 : engine == QVNT_ENGINE_PRECISION ? FMT_C32 : FMT_DF64;
+    return (engine == QVNT_ENGINE_PLAIN || engine == QVNT_ENGINE_TENSOR64) ? FMT_F64
+           : engine == QVNT_ENGINE_PRECISION                               ? FMT_C32
+                                                                           : FMT_DF64;
 }
 
 int make_reg(qvnt_ctx* ctx, uint32_t q_num, int engine, qvnt_reg** out) {
@@ -368,6 +375,18 @@ int qvnt_ctx_mem_info(qvnt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes
     return QVNT_OK;
 }
 
+int qvnt_ctx_set_engine(qvnt_ctx* ctx, int engine) {
+    CHECK_CTX(ctx);
+    if (!engine_valid(engine)) return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
+    std::lock_guard<std::mutex> lock(ctx->host_mu);
+    ctx->default_engine = engine;
+    if (ctx->host_reg) {  // the scratch register follows on the next qvnt_apply_host call
+        reg_free(ctx->host_reg);
+        ctx->host_reg = nullptr;
+    }
+    return QVNT_OK;
+}
+
 int qvnt_reg_create(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, qvnt_reg** out) {
     CHECK_CTX(ctx);
     return qvnt_reg_create_ex(ctx, q_num, state, ctx->default_engine, out);
@@ -377,8 +396,7 @@ int qvnt_reg_create_ex(qvnt_ctx* ctx, uint32_t q_num, uint64_t state, int engine
     CHECK_CTX(ctx);
     if (!out) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
     if (q_num > kMaxQubits) return set_error(QVNT_ERR_BAD_ARG, "q_num %u > %u", q_num, kMaxQubits);
-    if (engine != QVNT_ENGINE_FUSED && engine != QVNT_ENGINE_PLAIN && engine != QVNT_ENGINE_PRECISION)
-        return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
+    if (!engine_valid(engine)) return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
     qvnt_reg* r = nullptr;
     TRY(make_reg(ctx, q_num, engine, &r));
     const uint64_t q_mask = (1ull << q_num) - 1;
@@ -430,8 +448,7 @@ int qvnt_reg_len(const qvnt_reg* reg, uint64_t* len) {
 
 int qvnt_reg_set_engine(qvnt_reg* reg, int engine) {
     CHECK_REG(reg);
-    if (engine != QVNT_ENGINE_FUSED && engine != QVNT_ENGINE_PLAIN && engine != QVNT_ENGINE_PRECISION)
-        return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
+    if (!engine_valid(engine)) return set_error(QVNT_ERR_BAD_ARG, "unknown engine %d", engine);
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
     const int fmt = fmt_of_engine(engine);
     if (fmt_bytes(fmt) != fmt_bytes(reg->fmt)) {
@@ -477,6 +494,7 @@ int qvnt_reg_apply(qvnt_reg* reg, const qvnt_gate* gates, size_t count) {
     QVNT_CUDA_TRY(cudaSetDevice(reg->ctx->device));
     if (reg->engine == QVNT_ENGINE_PLAIN) return apply_plain(reg, gates, count);
     if (reg->engine == QVNT_ENGINE_PRECISION) return apply_precision(reg, gates, count);
+    if (reg->engine == QVNT_ENGINE_TENSOR64) return apply_tensor64(reg, gates, count);
     return apply_fused(reg, gates, count);
 }
 
@@ -707,7 +725,7 @@ int qvnt_apply_host(qvnt_ctx* ctx, const qvnt_gate* gates, size_t count, const d
         ctx->host_reg = nullptr;
     }
     if (!ctx->host_reg)
-        TRY(make_reg(ctx, q_num, ctx->default_engine == QVNT_ENGINE_PLAIN ? QVNT_ENGINE_PLAIN : QVNT_ENGINE_FUSED,
+        TRY(make_reg(ctx, q_num, ctx->default_engine == QVNT_ENGINE_PRECISION ? QVNT_ENGINE_FUSED : ctx->default_engine,
                      &ctx->host_reg));
     qvnt_reg* r = ctx->host_reg;
     for (size_t k = 0; k < count; ++k) {
@@ -719,7 +737,9 @@ int qvnt_apply_host(qvnt_ctx* ctx, const qvnt_gate* gates, size_t count, const d
     // left as IEEE f64 afterwards: the next call overwrites it).
     QVNT_CUDA_TRY(cudaMemcpyAsync(r->psi, psi_i, len * sizeof(amp_t), cudaMemcpyHostToDevice, r->stream));
     if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 1, r->stream));
-    TRY(r->engine == QVNT_ENGINE_PLAIN ? apply_plain(r, gates, count) : apply_fused(r, gates, count));
+    TRY(r->engine == QVNT_ENGINE_PLAIN      ? apply_plain(r, gates, count)
+        : r->engine == QVNT_ENGINE_TENSOR64 ? apply_tensor64(r, gates, count)
+                                            : apply_fused(r, gates, count));
     if (r->fmt == FMT_DF64) TRY(launch_convert(r->psi, r->len, 0, r->stream));
     QVNT_CUDA_TRY(cudaMemcpyAsync(psi_o, r->psi, len * sizeof(amp_t), cudaMemcpyDeviceToHost, r->stream));
     r->launches += r->fmt == FMT_DF64 ? 2 : 0;
@@ -865,6 +885,19 @@ int qvnt_precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_nu
         if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
     }
     return precision_plan_info(gates, count, q_num, passes, blocks);
+}
+
+int qvnt_tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* passes,
+                            uint64_t* plain_gates) {
+    if (!gates && count) return set_error(QVNT_ERR_BAD_ARG, "null gate list");
+    if (!passes || !plain_gates) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
+    if (q_num > kMaxQubits) return set_error(QVNT_ERR_BAD_ARG, "q_num %u > %u", q_num, kMaxQubits);
+    const uint64_t len = q_num < 3 ? 8 : 1ull << q_num;
+    for (size_t k = 0; k < count; ++k) {
+        int st = validate_gate(gates[k], len);
+        if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
+    }
+    return tensor64_plan_info(gates, count, (uint32_t)__builtin_ctzll(len), passes, plain_gates);
 }
 
 int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* passes) {

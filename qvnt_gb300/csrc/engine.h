@@ -75,5 +75,7 @@ int apply_plain(qvnt_reg* r, const qvnt_gate* gates, size_t count);
 int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count);
 int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count);
 int precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* blocks);
+int apply_tensor64(qvnt_reg* r, const qvnt_gate* gates, size_t count);
+int tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* plain_gates);
 int launch_inv(const double* d_abs, double* d_inv, int* d_status, cudaStream_t stream);
 }  // namespace qvnt

@@ -30,8 +30,10 @@
 #include <vector>
 
 #include "atomic.cuh"
+#include "dense_blocks.h"
 #include "engine.h"
 #include "kernels.h"
+#include "tc_ptx.cuh"
 
 #define TRY_LAUNCH(expr)        \
     do {                        \
@@ -44,8 +46,8 @@ namespace qvnt {
 namespace {
 
 constexpr int kPT = 13;            // tile qubits (at most; 12 for a 12-qubit register)
-constexpr int kBQ = 5;             // block qubits
-constexpr int kBD = 1 << kBQ;      // block dimension
+constexpr int kBQ = dense::kBQ;    // block qubits
+constexpr int kBD = dense::kBD;    // block dimension
 constexpr int kNT = 512;           // threads: 16 warps, four per tensor-memory lane quadrant
 constexpr int kMaxPB = 2;          // blocks per pass (their weights stay in shared memory)
 constexpr int kRenormEvery = 10;   // passes between FP64 norm restorations
@@ -75,68 +77,12 @@ struct PPassParams {
     PBlockDesc blocks[kMaxPB];
 };
 
-// ---- PTX helpers ---------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t it = 0; it < kPWaitLimit; ++it)
-        if (mbar_try(bar, parity)) return true;
-    return false;
-}
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
-                 "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
-                 : "memory");
-}
-__device__ __forceinline__ void tmem_relinquish() {
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: start address, LBO = 128 B, SBO = 2048 B, descriptor version 1,
-// no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(2048u >> 4) << 32) |
-           (1ull << 46);
-}
+// ---- PTX helpers (tc_ptx.cuh) --------------------------------------------------------------------
+using namespace tc;
+// Bounded wait with this engine's poll limit.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) { return tc::mbar_wait(bar, parity, kPWaitLimit); }
+// Operand descriptor: LBO = 128 B, SBO = 2048 B (64 TF32 values per row).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return tc::smem_desc(addr, 128u, 2048u); }
 
 // Instruction descriptor of kind::tf32: FP32 accumulator, A and B TF32 and K-major, N = 64, M = 128.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
@@ -151,33 +97,6 @@ __device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, ui
         "r"(a_tmem), "l"(b), "r"(kIdesc), "r"(accumulate)
         : "memory");
 }
-// 16 consecutive columns of this thread's lane.
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-        "%14, %15, %16};" ::"r"(taddr),
-        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
-        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
-        : "memory");
-}
-__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
-                 : "memory");
-}
-// 16 consecutive accumulator columns of this thread's lane.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-        : "r"(taddr)
-        : "memory");
-}
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
 __device__ __forceinline__ float tf32_rna(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -391,161 +310,11 @@ __global__ void __launch_bounds__(kNT, 1)
     if (warp == 0) tmem_dealloc(tmem_base, kCols);
 }
 
-// ---- host: dense gate matrices, blocks, passes ----------------------------------------------------
-struct Cd {
-    double re, im;
-};
-inline Cd cmul(Cd a, Cd b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
-inline Cd cadd(Cd a, Cd b) { return {a.re + b.re, a.im + b.im}; }
-
-inline uint64_t compress(uint64_t x, const std::vector<int>& sup) {  // global mask -> local bits
-    uint64_t r = 0;
-    for (size_t j = 0; j < sup.size(); ++j)
-        if ((x >> sup[j]) & 1ull) r |= 1ull << j;
-    return r;
-}
-
-struct LGate {
-    uint64_t sup = 0;     // global support mask (<= 5 bits)
-    std::vector<Cd> m;    // dense matrix over the support's local basis, row-major
-};
-
-// The dense matrix of one gate on its support, from qvnt's own atomic formulas (atomic.cuh) and the
-// control rule of dispatch.rs:32-47 (out[i] = f(psi, i) where i has every control bit, else psi[i]).
-int dense_gate(const qvnt_gate& g, LGate& out) {
-    uint64_t tg = g.a_mask;
-    if (g.kind == QVNT_GATE_H2 || g.kind == QVNT_GATE_U2) tg |= g.b_mask;
-    out.sup = tg | g.ctrl;
-    std::vector<int> sup;
-    for (int q = 0; q < 64; ++q)
-        if ((out.sup >> q) & 1ull) sup.push_back(q);
-    if (sup.size() > (size_t)kBQ)
-        return set_error(QVNT_ERR_UNSUPPORTED, "gate acts on %zu qubits (targets and controls); the precision engine "
-                                               "fuses at most %d", sup.size(), kBQ);
-    qvnt_gate lg = g;
-    lg.a_mask = compress(g.a_mask, sup);
-    lg.b_mask = compress(g.b_mask, sup);
-    lg.ctrl = compress(g.ctrl, sup);
-    const DevGate d = decode_gate(lg);
-    const uint64_t dim = 1ull << sup.size();
-    out.m.assign(dim * dim, Cd{0, 0});
-    std::vector<double2> col(dim);
-    for (uint64_t cidx = 0; cidx < dim; ++cidx) {
-        for (uint64_t i = 0; i < dim; ++i) col[i] = make_double2(i == cidx ? 1.0 : 0.0, 0.0);
-        auto psi = [&](uint64_t j) { return col[j]; };
-        for (uint64_t r = 0; r < dim; ++r) {
-            const double2 v = ((r & lg.ctrl) == lg.ctrl) ? atomic_op(d, r, psi) : col[r];
-            out.m[r * dim + cidx] = Cd{v.x, v.y};
-        }
-    }
-    return QVNT_OK;
-}
-
-// Gates as dense factors: the multi-bit X/Y/Z/S/T split into one-qubit factors (they commute), each
-// with the gate's controls.
-int lower_dense(const qvnt_gate* gates, size_t count, std::vector<LGate>& out) {
-    out.clear();
-    for (size_t i = 0; i < count; ++i) {
-        const qvnt_gate& g = gates[i];
-        if (g.kind == QVNT_GATE_ID) continue;
-        const bool multi = g.kind == QVNT_GATE_X || g.kind == QVNT_GATE_Y || g.kind == QVNT_GATE_Z ||
-                           g.kind == QVNT_GATE_S || g.kind == QVNT_GATE_T;
-        if (multi && __builtin_popcountll(g.a_mask) > 1) {
-            for (int q = 0; q < 64; ++q)
-                if ((g.a_mask >> q) & 1ull) {
-                    qvnt_gate f = g;
-                    f.a_mask = 1ull << q;
-                    LGate lg;
-                    const int st = dense_gate(f, lg);
-                    if (st) return set_error(st, "gate %zu: %s", i, qvnt_last_error());
-                    out.push_back(std::move(lg));
-                }
-            continue;
-        }
-        LGate lg;
-        const int st = dense_gate(g, lg);
-        if (st) return set_error(st, "gate %zu: %s", i, qvnt_last_error());
-        out.push_back(std::move(lg));
-    }
-    return QVNT_OK;
-}
-
-struct Block {
-    uint64_t sup = 0;        // exactly kBQ qubits
-    std::vector<Cd> u;       // 32 x 32, row-major, local bit j = j-th qubit of sup (ascending)
-};
-
-// U <- (M on the sub-support) * U, for a gate whose support lies inside the block's.
-void block_apply(Block& b, const LGate& g) {
-    std::vector<int> bq;
-    for (int q = 0; q < 64; ++q)
-        if ((b.sup >> q) & 1ull) bq.push_back(q);
-    std::vector<uint32_t> pos;  // local block bit of each gate-support qubit
-    for (int q = 0; q < 64; ++q)
-        if ((g.sup >> q) & 1ull) pos.push_back((uint32_t)(std::find(bq.begin(), bq.end(), q) - bq.begin()));
-    const uint32_t s = (uint32_t)pos.size(), dim = 1u << s;
-    uint32_t gm = 0;
-    for (uint32_t p : pos) gm |= 1u << p;
-    std::vector<uint32_t> dep(dim);
-    for (uint32_t x = 0; x < dim; ++x) {
-        uint32_t v = 0;
-        for (uint32_t j = 0; j < s; ++j)
-            if ((x >> j) & 1u) v |= 1u << pos[j];
-        dep[x] = v;
-    }
-    std::vector<Cd> tmp(dim);
-    for (uint32_t col = 0; col < (uint32_t)kBD; ++col)
-        for (uint32_t rest = 0; rest < (uint32_t)kBD; ++rest) {
-            if (rest & gm) continue;
-            for (uint32_t r = 0; r < dim; ++r) {
-                Cd acc{0, 0};
-                for (uint32_t cc = 0; cc < dim; ++cc)
-                    acc = cadd(acc, cmul(g.m[r * dim + cc], b.u[(rest | dep[cc]) * kBD + col]));
-                tmp[r] = acc;
-            }
-            for (uint32_t r = 0; r < dim; ++r) b.u[(rest | dep[r]) * kBD + col] = tmp[r];
-        }
-}
-
-void make_blocks(const std::vector<LGate>& lg, uint32_t L, std::vector<Block>& blocks) {
-    blocks.clear();
-    const size_t n = lg.size();
-    std::vector<char> done(n, 0);
-    size_t first = 0;
-    const uint64_t all = L >= 64 ? ~0ull : ((1ull << L) - 1ull);
-    while (true) {
-        while (first < n && done[first]) ++first;
-        if (first >= n) break;
-        uint64_t S = 0, blocked = 0;
-        std::vector<size_t> members;
-        size_t scanned = 0;
-        for (size_t j = first; j < n && scanned < 512; ++j) {
-            if (done[j]) continue;
-            ++scanned;
-            const uint64_t G = lg[j].sup;
-            if (!(G & blocked) && __builtin_popcountll(S | G) <= kBQ) {
-                S |= G;
-                members.push_back(j);
-                done[j] = 1;
-            } else {
-                blocked |= G;
-                if ((blocked & all) == all) break;
-            }
-        }
-        for (int q = 0; q < (int)L && __builtin_popcountll(S) < kBQ; ++q) S |= 1ull << q;  // pad to 5 qubits
-        Block b;
-        b.sup = S;
-        b.u.assign(kBD * kBD, Cd{0, 0});
-        for (int i = 0; i < kBD; ++i) b.u[i * kBD + i] = Cd{1, 0};
-        for (size_t j : members) block_apply(b, lg[j]);
-        blocks.push_back(std::move(b));
-    }
-}
-
-struct PPlan {
-    uint64_t qmask;
-    std::vector<size_t> members;  // block indices
-};
+// ---- host: dense blocks (dense_blocks.h) and their weights -----------------------------------------
+using dense::Block;
+using dense::Cd;
+using dense::LGate;
+using dense::PPlan;
 
 // Lowest qubits every pass keeps in its tile: 2^lowq contiguous amplitudes per TMA copy.  At most
 // 12 - 5 = 7, so that a block on five other qubits still fits an empty tile of a 12-qubit register.  Longer runs cost passes
@@ -562,37 +331,7 @@ uint32_t precision_lowq() {
 }
 
 int make_passes(const std::vector<Block>& blocks, uint32_t L, std::vector<PPlan>& passes) {
-    passes.clear();
-    const int kt = std::min<int>(kPT, (int)L);  // tile qubits
-    const size_t n = blocks.size();
-    std::vector<char> done(n, 0);
-    size_t first = 0;
-    const uint64_t low = (1ull << precision_lowq()) - 1ull;
-    while (true) {
-        while (first < n && done[first]) ++first;
-        if (first >= n) break;
-        PPlan p;
-        uint64_t Q = low & ((L >= 64) ? ~0ull : ((1ull << L) - 1ull)), blocked = 0;
-        size_t scanned = 0;
-        for (size_t j = first; j < n && scanned < 64 && p.members.size() < (size_t)kMaxPB; ++j) {
-            if (done[j]) continue;
-            ++scanned;
-            const uint64_t S = blocks[j].sup;
-            if (!(S & blocked) && __builtin_popcountll(Q | S) <= kt) {
-                Q |= S;
-                p.members.push_back(j);
-                done[j] = 1;
-            } else {
-                blocked |= S;
-            }
-        }
-        if (p.members.empty())  // cannot happen with lowq <= 7: a block always fits an empty tile
-            return set_error(QVNT_ERR_UNSUPPORTED, "precision planner could not place block %zu", first);
-        for (uint32_t q = 0; q < L && __builtin_popcountll(Q) < kt; ++q) Q |= 1ull << q;
-        p.qmask = Q;
-        passes.push_back(std::move(p));
-    }
-    return QVNT_OK;
+    return dense::make_passes(blocks, L, kPT, precision_lowq(), (size_t)kMaxPB, passes);
 }
 
 // TF32 rounding to nearest (ties away from zero), as cvt.rna.tf32.f32 does on the device.
@@ -631,11 +370,11 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
     if (L < 12) return set_error(QVNT_ERR_UNSUPPORTED, "the precision engine needs at least 12 qubits");
     std::vector<LGate> lg;
-    int st = lower_dense(gates, count, lg);
+    int st = dense::lower_dense(gates, count, lg);
     if (st) return st;
     if (lg.empty()) return QVNT_OK;
     std::vector<Block> blocks;
-    make_blocks(lg, L, blocks);
+    dense::make_blocks(lg, L, blocks);
     std::vector<PPlan> passes;
     st = make_passes(blocks, L, passes);
     if (st) return st;
@@ -711,10 +450,10 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
 
 int precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* blocks) {
     std::vector<LGate> lg;
-    int st = lower_dense(gates, count, lg);
+    int st = dense::lower_dense(gates, count, lg);
     if (st) return st;
     std::vector<Block> bl;
-    make_blocks(lg, L, bl);
+    dense::make_blocks(lg, L, bl);
     std::vector<PPlan> ps;
     st = make_passes(bl, L, ps);
     if (st) return st;

@@ -31,6 +31,10 @@ class Context:
         check(lib().qvnt_ctx_mem_info(self.h, ctypes.byref(f), ctypes.byref(t)))
         return f.value, t.value
 
+    def set_engine(self, engine):
+        """Engine of the registers QReg makes on this context by default and of apply_host."""
+        check(lib().qvnt_ctx_set_engine(self.h, engine))
+
     def apply_host(self, ops, psi_i, psi_o=None):
         """`Applicable::apply(psi_i, psi_o)` (src/operator/applicable.rs:5-6) on host buffers:
         psi_i / psi_o are complex128 arrays (len a power of two >= 8)."""
