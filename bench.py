@@ -1,22 +1,29 @@
 """Benchmark: 30-qubit f64 random circuit (depth 40 + qft) on one GB300, qvnt semantics.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--engine tensor64|plain|fused]
 
 A step is one run of the workload circuit on a resident 30-qubit register: reset to |0> and
-apply the 2,985-gate queue (40 layers of {h, s, t, u3} on every qubit, 15 random two-qubit gates
+apply the 2,967-gate queue (40 layers of {h, s, t, u3} on every qubit, 15 random two-qubit gates
 from {rxx, ryy, rzz, swap, i_swap, sqrt_i_swap}, 3 Toffolis, then qft over all 30 qubits).
 Inputs are seeded synthetic circuits (no public suite).  The state (16 GiB) is larger than L2
 (129 MB), so no flush is needed between steps.
 
-Printed as one JSON line (rank 0):
+The headline engine is TENSOR64: IEEE f64 amplitudes, gates fused into dense 5-qubit blocks and
+contracted on the tensor cores with 53-bit operands split into exact fp16 digit products (no FP64
+instruction, one f64 rounding per block).  Printed as one JSON line (rank 0):
   value        unfused gate passes per second (qvnt SingleOps), whole job, device-timed
   e2e          the same metric through the plugin call qvnt_apply_host (Applicable::apply): the
                state goes host -> device -> host from pinned memory inside the timed region
-  roofline     the fused-pass kernel: algorithmic bytes (2 x 2^30 x 16 B per pass) / its average
-               CUDA-event duration, against the measured HBM copy bandwidth
-  cpu_baseline the CPU oracle (qvnt's algorithm restated in C, OpenMP on every host core) on a
-               bounded sample of the same circuit at 30 qubits
---impl reference times only that CPU implementation (the reference is Rust; no cargo exists here).
+  roofline     the engine's pass kernel: algorithmic bytes (2 x 2^30 x 16 B per pass) / its
+               average CUDA-event duration, against the measured HBM copy bandwidth
+  plain_f64_gpu the PLAIN engine (one IEEE f64 pass per SingleOp, bit-identical to qvnt) on the
+               same circuit
+  cpu_baseline the CPU oracle (qvnt's algorithm restated in C: one out-of-place gather pass per
+               gate, OpenMP on every host core) timed per gate on a stratified sample of the same
+               circuit at 30 qubits (1-qubit gates, 2-qubit gates, Toffolis, QFT rotations)
+  forms        the double-float fused engine (df64), the batching, serving and precision forms
+--impl reference times only that CPU implementation (the reference is Rust; no cargo exists here),
+with the circuit built by the oracle's own builders, so no engine code runs in that process.
 With N > 1 (torchrun) each rank runs an independent replica on its own GPU ("replicas only").
 """
 import argparse
@@ -38,7 +45,18 @@ N_QUBITS = 30
 DEPTH = 40
 SEED = 2
 AMP_BYTES = 16
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "fused_pass_traffic.json")
+PROFILE_TRAFFIC = {"fused": os.path.join(ROOT, "profiles", "fused_pass_traffic.json"),
+                   "tensor64": os.path.join(ROOT, "profiles", "tensor64_pass_traffic.json")}
+KERNEL = {"tensor64": "tensor64_pass_kernel", "fused": "fused_df_kernel", "plain": "plain_gate_kernel"}
+ARITHMETIC = {
+    "tensor64": "IEEE f64 storage; dense 5-qubit blocks on tcgen05 with 53-bit operands split into 7 exact fp16 "
+                "digits (28 digit products, FP32 accumulation of integers below 2^23, exact), integer "
+                "reconstruction and one rounding to f64 per block; no FP64 instruction",
+    "plain": "IEEE f64, one pass per SingleOp in qvnt's operand order, bit-identical to the oracle",
+    "fused": "double-float (pairs of FP32 with error-free transforms, 48-bit significand, FP32 exponent range) on "
+             "the FP32 pipes, within 1e-12 of the IEEE f64 oracle",
+}
+DTYPE = {"tensor64": "f64", "plain": "f64", "fused": "df64 (2 x f32, 48-bit significand)"}
 
 
 def parse():
@@ -49,15 +67,16 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--depth", type=int, default=DEPTH)
-    ap.add_argument("--engine", default="fused", choices=["fused", "plain"])
+    ap.add_argument("--engine", default="tensor64", choices=["tensor64", "plain", "fused"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1, help="steps of the plain f64 GPU path (0 = skip)")
-    ap.add_argument("--forms", default="batch,serve,precision",
-                    help="extra forms to measure: batch, serve, precision (empty = none)")
+    ap.add_argument("--forms", default="df64,batch,serve,precision",
+                    help="extra forms to measure: df64, batch, serve, precision (empty = none)")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--cpu-per-class", type=int, default=3, help="gates per stratum in the cpu_baseline sample")
     return ap.parse_args()
 
 
@@ -160,26 +179,58 @@ def algorithmic_pass_bytes(n):
     return 2 * (1 << n) * AMP_BYTES
 
 
-def cpu_sample(circ_gates, n, budget_s=12.0):
-    """The oracle (qvnt's algorithm: one out-of-place gather pass per gate, OpenMP over amplitudes)
-    on the first gates of the same circuit at the same register size; returns (gates/s, threads,
-    gates timed)."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import numpy as np
-    import oracle_ref as orc
-    threads = orc.max_threads()
-    psi = orc.new_state(n, 0)
-    scratch = np.empty_like(psi)
-    arr = orc.arr(circ_gates)
-    lib = orc.lib()
-    done, t_total = 0, 0.0
-    # one gate at a time, until the budget is spent
-    while done < len(circ_gates) and t_total < budget_s:
+def workload_config(n, depth, gates, ws):
+    """The workload's description, identical in both arms (ours and --impl reference)."""
+    return {"workload": "random circuit %dq f64, depth %d + qft, %d gates" % (n, depth, gates), "n_qubits": n,
+            "depth": depth, "seed": SEED, "gates": gates, "parallelism": "replicas" if ws > 1 else "single",
+            "l2": "state %d GiB > L2 129 MB, no flush" % ((1 << n) * AMP_BYTES >> 30)}
+
+
+class CpuSampler:
+    """The oracle (qvnt's algorithm: one out-of-place gather pass per gate over every amplitude,
+    src/operator/atomic/dispatch.rs:50-67, OpenMP over all host threads) timed gate by gate on a
+    stratified sample of the circuit: `per_class` gates from each of its strata (1-qubit gates,
+    2-qubit gates, Toffolis, QFT controlled rotations), spread over the whole circuit and different
+    on every call; the circuit's time is estimated as sum over strata of (gates in the stratum) x
+    (mean sampled time).  The circuit is built with the oracle's own builders.  Returns gate passes
+    per second, threads and a description of the sample."""
+
+    def __init__(self, n, depth, seed):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import numpy as np
+        import oracle_ref as orc
+        self.orc, self.n = orc, n
+        self.gates = orc.random_circuit_gates(n, depth, seed=seed)
+        self.arr = orc.arr(self.gates)
+        self.strata = {}
+        for i, g in enumerate(self.gates):
+            self.strata.setdefault(orc.gate_class(g), []).append(i)
+        self.threads = orc.max_threads()
+        self.cur = orc.new_state(n, 0)
+        self.nxt = np.zeros_like(self.cur)  # touched once here, outside any timed pass
+        self.calls = 0
+
+    def _pass(self, i):
         t0 = time.perf_counter()
-        lib.oracle_apply(ctypes.byref(arr[done]), 1, psi.ctypes.data, scratch.ctypes.data, psi.size, threads)
-        t_total += time.perf_counter() - t0
-        done += 1
-    return done / t_total, threads, done
+        self.orc.lib().oracle_for_each(ctypes.byref(self.arr[i]), self.cur.ctypes.data, self.nxt.ctypes.data,
+                                       self.cur.size, self.threads)
+        dt = time.perf_counter() - t0
+        self.cur, self.nxt = self.nxt, self.cur
+        return dt
+
+    def sample(self, per_class):
+        est, timed, counts = 0.0, 0, {}
+        for name in sorted(self.strata):
+            idx = self.strata[name]
+            picks = [idx[((self.calls * per_class + k) * 7919 + len(idx) // 2) % len(idx)] for k in range(per_class)]
+            ts = [self._pass(i) for i in picks]
+            est += len(idx) * sum(ts) / len(ts)
+            timed += len(ts)
+            counts[name] = len(idx)
+        self.calls += 1
+        desc = ("%d gate passes timed at %d qubits, %d per stratum of %s, circuit time = sum of stratum size x mean "
+                "sampled pass time" % (timed, self.n, per_class, counts))
+        return len(self.gates) / est, self.threads, desc
 
 
 def bench_batch(ctx, count, steps):
@@ -237,11 +288,11 @@ def bench_batch(ctx, count, steps):
 def bench_precision(ctx, n=32, depth=60, n_ref=30):
     """Precision form: complex<f32> register of n qubits (32 GiB at 32), the random-layer generator
     at depth 60, dense 5-qubit blocks on the tensor cores with FP64 norm restoration every 10
-    passes.  Fidelity defect and max-abs error against the double-float engine (f64-equivalent,
-    within 1e-12 of the oracle) at n_ref qubits with the same seed; the plain f64 GPU path at n
-    qubits timed on the first 64 gates and extrapolated per gate."""
+    passes.  Fidelity defect and max-abs error against the PLAIN IEEE f64 engine (bit-identical to
+    the oracle) at n_ref qubits with the same seed; the plain f64 GPU path at n qubits timed on the
+    first 64 gates and extrapolated per gate."""
     import torch
-    from qvnt_gb300 import ENGINE_FUSED, ENGINE_PLAIN, ENGINE_PRECISION, QReg
+    from qvnt_gb300 import ENGINE_PLAIN, ENGINE_PRECISION, QReg
     from qvnt_gb300.circuits import SplitMix64, random_layers_gates
 
     def gates(m):
@@ -279,11 +330,11 @@ def bench_precision(ctx, n=32, depth=60, n_ref=30):
     plain_ms_per_gate = f0.elapsed_time(f1) / sample
     qp.close()
     del qp
-    # fidelity at n_ref qubits against the f64-equivalent engine
+    # fidelity at n_ref qubits against IEEE f64 (the plain engine, bit-identical to the oracle)
     arr_r, cnt_r = gates(n_ref)
     a = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_PRECISION)
     a.apply_gates(arr_r, cnt_r)
-    b = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_FUSED)
+    b = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_PLAIN)
     b.apply_gates(arr_r, cnt_r)
     fid, mx = a.overlap(b)
     a.close()
@@ -294,6 +345,7 @@ def bench_precision(ctx, n=32, depth=60, n_ref=30):
             "circuits_per_s": 1e3 / ms, "ms_per_circuit": ms, "gate_passes_per_s": cnt / (ms / 1e3),
             "passes": p1 - p0, "kernel_avg_ms": avg, "kernel_gbs": pass_bytes / (avg / 1e3) / 1e9,
             "fidelity_defect_vs_f64": 1.0 - fid, "max_abs_err_vs_f64": mx, "fidelity_qubits": n_ref,
+            "fidelity_reference": "PLAIN engine (IEEE f64, bit-identical to the oracle), same seed, %d gates" % cnt_r,
             "plain_f64_gpu": {"circuits_per_s": 1e3 / (plain_ms_per_gate * cnt),
                               "sample": "first %d gates at %d qubits, extrapolated per gate" % (sample, n)}}
 
@@ -338,32 +390,63 @@ def bench_serve(ctx, rate, seconds):
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: qvnt's CPU algorithm on the host cores (the C restatement; the Rust crate
-    cannot be built here), rank 0 only."""
+    """--impl reference: qvnt's CPU algorithm on the host cores (the C restatement of the oracle;
+    the Rust crate cannot be built here), rank 0 only.  Each step times one stratified sample of the
+    workload's gate passes (about 8 s); nothing of the engine library is loaded."""
     if rank != 0:
         return
-    from qvnt_gb300.circuits import random_circuit
-    circ = random_circuit(args.qubits, args.depth, seed=SEED)
-    gates = circ.gates()
-    vals = []
-    threads = 1
+    sampler = CpuSampler(args.qubits, args.depth, SEED)
+    vals, walls, desc, threads = [], [], "", 1
     for i in range(args.warmup + args.steps):
-        v, threads, done = cpu_sample(gates, args.qubits, budget_s=8.0)
+        t0 = time.perf_counter()
+        v, threads, desc = sampler.sample(1)
         if i >= args.warmup:
             vals.append(v)
+            walls.append(time.perf_counter() - t0)
     value = sum(vals) / len(vals)
     unit = "gate-passes/s"
     line = {
         "impl": "reference", "metric": "%dq gate-passes/s" % args.qubits, "value": value, "unit": unit,
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64 circuit)",
-        "config": {"workload": "random circuit %dq depth %d + qft, %d gates" % (args.qubits, args.depth, len(gates)),
-                   "n_qubits": args.qubits, "depth": args.depth, "gates": len(gates)},
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(walls) / len(walls) * 1e3,
+        "ms_per_circuit_estimate": len(sampler.gates) / value * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded SplitMix64 random circuit)",
+        "config": workload_config(args.qubits, args.depth, len(sampler.gates), ws),
         "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port",
-                         "sample": "first gates of the circuit, ~8 s per step, at %d qubits" % args.qubits},
+                         "sample": "per step: " + desc + "; value = mean over steps"},
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def bench_df64(ctx, circ_arr, ngates, n, steps):
+    """The double-float fused engine (48-bit significand, FP32 exponent range: narrower than IEEE
+    f64) on the same circuit: gate passes/s and its per-pass HBM roofline."""
+    import torch
+    from qvnt_gb300 import ENGINE_FUSED, QReg
+    q = QReg(n, 0, ctx=ctx)
+    q.set_engine(ENGINE_FUSED)
+    s = torch.cuda.ExternalStream(q.stream())
+    q.reset(0)
+    q.apply_gates(circ_arr, ngates)
+    q.sync()
+    _, p0 = q.stats()
+    q.kernel_timing(enable=1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        q.reset(0)
+        q.apply_gates(circ_arr, ngates)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kms, kn = q.kernel_timing(enable=0)
+    _, p1 = q.stats()
+    q.close()
+    avg = kms / kn if kn else None
+    return {"value": ngates * steps / (ms / 1e3), "unit": "gate-passes/s", "ms_per_step": ms / steps, "steps": steps,
+            "dtype": DTYPE["fused"], "arithmetic": ARITHMETIC["fused"], "passes_per_step": (p1 - p0) / steps,
+            "kernel": KERNEL["fused"], "avg_launch_ms": avg,
+            "kernel_gbs": algorithmic_pass_bytes(n) / (avg / 1e3) / 1e9 if avg else None}
 
 
 def main():
@@ -374,7 +457,7 @@ def main():
         return
     import numpy as np
     import torch
-    from qvnt_gb300 import ENGINE_FUSED, ENGINE_PLAIN, Context, QReg
+    from qvnt_gb300 import ENGINE_FUSED, ENGINE_PLAIN, ENGINE_TENSOR64, Context, QReg
     from qvnt_gb300._abi import gate_array
     from qvnt_gb300.circuits import random_circuit
 
@@ -386,7 +469,8 @@ def main():
     gates = circ.gates()
     garr = gate_array(gates)
     ngates = len(gates)
-    engine = ENGINE_FUSED if args.engine == "fused" else ENGINE_PLAIN
+    engines = {"tensor64": ENGINE_TENSOR64, "plain": ENGINE_PLAIN, "fused": ENGINE_FUSED}
+    engine = engines[args.engine]
 
     q = QReg(n, 0, ctx=ctx)
     q.set_engine(engine)
@@ -425,7 +509,11 @@ def main():
     units = ngates * args.steps * ws
     value = units / (ms_max / 1e3)
     pass_bytes = algorithmic_pass_bytes(n)
-    hbm_gbs = passes_per_step * args.steps * pass_bytes / (dev_ms / 1e3) / 1e9
+    if engine == ENGINE_PLAIN:  # one pass per gate over the 2^(n - controls) amplitudes it touches
+        step_bytes = sum(2 * (1 << (n - bin(g.ctrl).count("1"))) * AMP_BYTES for g in gates if g.kind != 0)
+    else:
+        step_bytes = passes_per_step * pass_bytes
+    hbm_gbs = step_bytes * args.steps / (dev_ms / 1e3) / 1e9
 
     peaks = {}
     try:
@@ -438,18 +526,20 @@ def main():
     if not peak:
         peak = 6800.0
     avg_launch_ms = kern_ms / kern_n if kern_n else None
-    achieved = pass_bytes / (avg_launch_ms / 1e3) / 1e9 if avg_launch_ms else None
+    if engine == ENGINE_PLAIN:
+        achieved = step_bytes * args.steps / (kern_ms / 1e3) / 1e9 if kern_ms else None
+    else:
+        achieved = pass_bytes / (avg_launch_ms / 1e3) / 1e9 if avg_launch_ms else None
     traffic = None
     try:
-        with open(PROFILE_TRAFFIC) as f:
-            tr = json.load(f)
-        traffic = tr.get("bytes_per_full_launch_%dq" % n)
+        with open(PROFILE_TRAFFIC[args.engine]) as f:
+            traffic = json.load(f).get("bytes_per_full_launch_%dq" % n)
     except Exception:
         pass
 
     # plain f64 GPU path on the same workload (one pass per SingleOp), for the comparison the metric names
     plain = None
-    if args.plain_steps > 0 and engine == ENGINE_FUSED:
+    if args.plain_steps > 0 and engine != ENGINE_PLAIN:
         qp = QReg(n, 0, ctx=ctx)
         qp.set_engine(ENGINE_PLAIN)
         sp = torch.cuda.ExternalStream(qp.stream())
@@ -465,7 +555,8 @@ def main():
         torch.cuda.synchronize()
         pms = e0.elapsed_time(e1)
         plain = {"value": ngates * args.plain_steps / (pms / 1e3), "unit": "gate-passes/s",
-                 "ms_per_step": pms / args.plain_steps, "steps": args.plain_steps}
+                 "ms_per_step": pms / args.plain_steps, "steps": args.plain_steps, "dtype": "f64",
+                 "arithmetic": ARITHMETIC["plain"]}
         qp.close()
         del qp
 
@@ -475,6 +566,7 @@ def main():
         q.close()
         del q
         torch.cuda.synchronize()
+        ctx.set_engine(engine)
         length = max(1 << n, 8)
         hin = torch.zeros(length * 2, dtype=torch.float64, pin_memory=True)
         hout = torch.empty(length * 2, dtype=torch.float64, pin_memory=True)
@@ -495,7 +587,7 @@ def main():
         e2e_s = dist.max(time.perf_counter() - t0)
         e2e = {"value": ngates * args.steps * ws / e2e_s, "unit": "gate-passes/s",
                "h2d_bytes_per_step": length * AMP_BYTES + ngates * ctypes.sizeof(gates[0]),
-               "d2h_bytes_per_step": length * AMP_BYTES}
+               "d2h_bytes_per_step": length * AMP_BYTES, "engine": args.engine}
 
     forms = {}
     if args.no_e2e:  # the e2e leg has already released the 30-qubit register
@@ -505,13 +597,16 @@ def main():
         torch.cuda.synchronize()
         for form in [f for f in args.forms.split(",") if f]:
             try:
-                if form == "batch":
-                    forms["batch"] = bench_batch(ctx, args.batch_count, max(1, args.steps))
+                if form == "df64":
+                    if engine != ENGINE_FUSED:
+                        forms["df64"] = bench_df64(ctx, garr, ngates, n, max(1, min(args.steps, 3)))
+                elif form == "batch":
+                    forms["batch"] = bench_batch(ctx, args.batch_count, max(1, min(args.steps, 5)))
                 elif form == "serve":
                     forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds)
                     # the same request mix at a rate one GPU sustains (the configured rate is about
                     # two orders of magnitude above its capacity for this mix)
-                    forms["serve"]["at_sustainable_rate"] = bench_serve(ctx, 4.0, args.serve_seconds)
+                    forms["serve"]["at_sustainable_rate"] = bench_serve(ctx, 4.0, min(args.serve_seconds, 20.0))
                 elif form == "precision":
                     forms["precision"] = bench_precision(ctx)
             except Exception as exc:  # a form's failure is reported, not hidden
@@ -519,11 +614,19 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, threads, done = cpu_sample(gates, n)
-        cpu = {"value": v, "unit": "gate-passes/s", "cores": threads, "kind": "port",
-               "sample": "first %d gates of the circuit at %d qubits (oracle, OpenMP)" % (done, n)}
+        sampler = CpuSampler(n, args.depth, SEED)
+        v, threads, desc = sampler.sample(args.cpu_per_class)
+        cpu = {"value": v, "unit": "gate-passes/s", "cores": threads, "kind": "port", "sample": desc}
+        del sampler
 
     if rank == 0:
+        regime = {
+            "tensor64": "one pass per dense 5-qubit block: TMA tile loads/stores overlap the digit products on "
+                        "the tensor cores and the integer slicing/reconstruction on the CUDA cores",
+            "fused": "compute-bound: double-float arithmetic on the FP32/ALU pipes",
+            "plain": "one pass per gate; rotations bound by the FP64 pipe (about 1.6 FP64 ops/clk/SM), "
+                     "permutations by HBM; achieved = all gates' algorithmic bytes over their kernel time",
+        }[args.engine]
         line = {
             "metric": "%dq gate-passes/s" % n,
             "value": value,
@@ -535,26 +638,19 @@ def main():
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64",
+            "dtype": DTYPE[args.engine],
             "data": "synthetic (seeded SplitMix64 random circuit)",
-            "config": {"workload": "random circuit %dq f64, depth %d + qft, %d gates" % (n, args.depth, ngates),
-                       "n_qubits": n, "depth": args.depth, "gates": ngates, "engine": args.engine,
-                       "fused_passes_per_step": passes_per_step,
-                       "arithmetic": "double-float (pairs of FP32 with error-free transforms, 48-bit significand) on "
-                                     "the FP32 pipes, within 1e-12 of the IEEE f64 oracle" if engine == ENGINE_FUSED
-                                     else "IEEE f64, bit-identical to the oracle",
-                       "parallelism": "replicas" if ws > 1 else "single",
-                       "l2": "state %d GiB > L2 129 MB, no flush" % ((1 << n) * AMP_BYTES >> 30)},
+            "config": workload_config(n, args.depth, ngates, ws),
+            "engine": args.engine,
+            "arithmetic": ARITHMETIC[args.engine],
+            "passes_per_step": passes_per_step,
             "hbm_gbs": hbm_gbs,
             "circuits_per_s": ws * args.steps / (ms_max / 1e3),
             "wall_s": wall,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "peak_source": peak_src, "kernel": "fused_df_kernel" if engine == ENGINE_FUSED else "plain_gate_kernel",
-                         "launches_timed": kern_n, "avg_launch_ms": avg_launch_ms,
-                         "regime": "compute-bound: double-float arithmetic on the FP32/ALU pipes; achieved is one "
-                                   "pass's algorithmic bytes over its duration, and a pass carries ~18 gates "
-                                   "at the default pass budget (800)"},
+                         "peak_source": peak_src, "kernel": KERNEL[args.engine],
+                         "launches_timed": kern_n, "avg_launch_ms": avg_launch_ms, "regime": regime},
             "plain_f64_gpu": plain,
             "cpu_baseline": cpu,
             "e2e": e2e,

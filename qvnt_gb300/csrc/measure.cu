@@ -677,6 +677,11 @@ using namespace qvnt;
 // is looked up once per device (with that device current) and cached.
 extern "C" int qvnt_norm_sqr_noalloc(const double* d_psi, uint64_t len, double* d_out, void* stream) {
     if (!d_psi || !d_out) return set_error(QVNT_ERR_BAD_ARG, "null device pointer");
+    // the kernels read amplitudes as 16-byte double2 and write *d_out as a double: a misaligned
+    // pointer would fault the caller's context, so it is refused here
+    if (reinterpret_cast<uintptr_t>(d_psi) & 15u)
+        return set_error(QVNT_ERR_BAD_ARG, "d_psi is not 16-byte aligned (amplitudes are read as double2)");
+    if (reinterpret_cast<uintptr_t>(d_out) & 7u) return set_error(QVNT_ERR_BAD_ARG, "d_out is not 8-byte aligned");
     if (len == 0) return set_error(QVNT_ERR_BAD_ARG, "empty state");
     if (len > QVNT_NOALLOC_MAX_AMPLITUDES)
         return set_error(QVNT_ERR_BAD_ARG, "state of %llu amplitudes exceeds the allocation-free limit of %llu",

@@ -22,6 +22,7 @@ c_u32, c_u64, c_int, c_double, c_size, c_void = (ctypes.c_uint32, ctypes.c_uint6
 
 _PROTOS = {
     "oracle_acts_on": (c_u64, [P(QvntGate)]),
+    "oracle_for_each": (None, [P(QvntGate), c_void, c_void, c_u64, c_int]),
     "oracle_apply": (None, [P(QvntGate), c_size, c_void, c_void, c_u64, c_int]),
     "oracle_reg_len": (c_u64, [c_u32]),
     "oracle_reg_init": (None, [c_u32, c_u64, c_void]),
@@ -213,3 +214,108 @@ def linear_composition(psi, other, c0, c1):
 
 def max_threads():
     return lib().oracle_max_threads()
+
+
+# ---- workloads built by the oracle's own builders ---------------------------------------------
+# The seeded circuits of qvnt_gb300.circuits, drawn from the same SplitMix64 stream but built with
+# the oracle's restatement of qvnt's constructors (oracle_gate_make, oracle_op_h/u3/qft,
+# oracle_gate_c).  The CPU baseline and the reference arm of the benchmark use these, so that no
+# code of the engine library runs on their path; a CPU test checks that both builders give the
+# same gate list byte for byte.
+_M64 = (1 << 64) - 1
+TWO_PI = 2.0 * 3.141592653589793
+
+
+class SplitMix64:
+    def __init__(self, seed):
+        self.state = seed & _M64
+
+    def next_u64(self):
+        self.state = (self.state + 0x9E3779B97F4A7C15) & _M64
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        return z ^ (z >> 31)
+
+    def uniform(self):
+        return (self.next_u64() >> 11) * (1.0 / 9007199254740992.0)
+
+    def below(self, n):
+        return self.next_u64() % n
+
+
+def random_layers_gates(n, depth, rng):
+    """Per layer: one of {h, s, t, u3} on every qubit, 15 two-qubit gates from {rxx, ryy, rzz, swap,
+    i_swap, sqrt_i_swap} on random distinct pairs, 3 Toffolis x(t).c(c1 | c2)."""
+    out = []
+    for _ in range(depth):
+        for q in range(n):
+            kind = rng.below(4)
+            m = 1 << q
+            if kind == 0:
+                out += op_h(m)
+            elif kind == 1:
+                out.append(make("S", m))
+            elif kind == 2:
+                out.append(make("T", m))
+            else:
+                th, ph, la = TWO_PI * rng.uniform(), TWO_PI * rng.uniform(), TWO_PI * rng.uniform()
+                out += op_u3(th, ph, la, m)
+        for _ in range(15):
+            a = rng.below(n)
+            b = rng.below(n - 1)
+            if b >= a:
+                b += 1
+            ab = (1 << a) | (1 << b)
+            kind = rng.below(6)
+            if kind < 3:
+                out.append(make(("RXX", "RYY", "RZZ")[kind], ab, angle=TWO_PI * rng.uniform()))
+            else:
+                out.append(make(("SWAP", "ISWAP", "SQRT_ISWAP")[kind - 3], ab))
+        for _ in range(3):
+            t = rng.below(n)
+            c1 = rng.below(n - 1)
+            if c1 >= t:
+                c1 += 1
+            c2 = rng.below(n)
+            while c2 == t or c2 == c1:
+                c2 = rng.below(n)
+            out.append(c(make("X", 1 << t), (1 << c1) | (1 << c2)))
+    return out
+
+
+def random_circuit_gates(n=30, depth=40, seed=2, with_qft=True):
+    """The random circuit: random layers, then op::qft over all n qubits."""
+    out = random_layers_gates(n, depth, SplitMix64(seed))
+    if with_qft:
+        out += op_qft((1 << n) - 1)
+    return out
+
+
+def plain_circuit_gates(n=20, layers=20, seed=1):
+    """op::h(all), then per layer rx, ry, rz on every qubit and nearest-neighbour CNOTs at an
+    alternating offset, then op::qft(all)."""
+    rng = SplitMix64(seed)
+    out = op_h((1 << n) - 1)
+    for layer in range(layers):
+        for q in range(n):
+            out.append(make("RX", 1 << q, angle=TWO_PI * rng.uniform()))
+            out.append(make("RY", 1 << q, angle=TWO_PI * rng.uniform()))
+            out.append(make("RZ", 1 << q, angle=TWO_PI * rng.uniform()))
+        for i in range(layer % 2, n - 1, 2):
+            out.append(c(make("X", 1 << (i + 1)), 1 << i))
+    return out + op_qft((1 << n) - 1)
+
+
+def gate_class(g):
+    """Stratum of a gate of these workloads, for sampled timings: 'qft' (controlled RZ), 'toffoli'
+    (X with controls), 'two' (two-qubit kinds), 'one' (the rest)."""
+    k = g.kind
+    if g.ctrl and k == KIND["RZ"]:
+        return "qft"
+    if g.ctrl:
+        return "toffoli"
+    if k in (KIND["RXX"], KIND["RYY"], KIND["RZZ"], KIND["SWAP"], KIND["ISWAP"], KIND["SQRT_ISWAP"],
+             KIND["SQRT_SWAP"], KIND["H2"], KIND["U2"]):
+        return "two"
+    return "one"

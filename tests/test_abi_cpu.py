@@ -238,3 +238,24 @@ int main(void) {
     run = subprocess.run([str(exe)], capture_output=True, text=True)
     assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
     assert run.stdout.startswith("C3_X4 10 ")
+
+
+def test_norm_noalloc_argument_checks_without_gpu(lib_built):
+    """qvnt_norm_sqr_noalloc refuses misaligned, null and oversized arguments on the host, before any
+    CUDA call (dummy pointers: nothing is dereferenced)."""
+    import ctypes
+
+    from qvnt_gb300 import _abi
+
+    f = lib_built.qvnt_norm_sqr_noalloc
+    cases = [
+        (0x1008, 64, 0x2000, b"16-byte aligned"),   # d_psi only 8-byte aligned
+        (0x1000, 64, 0x2004, b"8-byte aligned"),    # d_out misaligned
+        (0, 64, 0x2000, b"null"),
+        (0x1000, 0, 0x2000, b"empty"),
+        (0x1000, (1 << 28) + 1, 0x2000, b"allocation-free limit"),
+    ]
+    for psi, n, out, msg in cases:
+        st = f(ctypes.c_void_p(psi), n, ctypes.c_void_p(out), None)
+        assert st == _abi.ERR_BAD_ARG, (psi, n, out)
+        assert msg in lib_built.qvnt_last_error(), lib_built.qvnt_last_error()

@@ -2,7 +2,8 @@
 
 Bar: the PLAIN engine (one pass per SingleOp, qvnt's operand order, no FMA contraction) is
 bit-identical to the oracle; the FUSED engine agrees within 1e-12 max-abs on every amplitude
-(the f64 tolerance this engine is built to).  Measured indices are identical given the same draw,
+(the f64 tolerance this engine is built to) and within REL of the largest amplitude, a bound set
+from its measured error so that a loss of a few bits fails.  Measured indices are identical given the same draw,
 except where the draw falls within 1e-12 of a cumulative-probability boundary.
 """
 import math
@@ -18,7 +19,15 @@ from qvnt_gb300.operator import MultiOp, SingleOp
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+REL = 2e-13
 ENGINES = [ENGINE_PLAIN, ENGINE_FUSED]
+
+
+def assert_close(got, want):
+    """max|got - want| <= TOL and <= REL * max|want|."""
+    d = float(np.max(np.abs(got - want)))
+    scale = float(np.max(np.abs(want)))
+    assert d <= TOL and d <= REL * scale, (d, d / scale if scale else d)
 
 
 def run_gpu(n, state, circuit, engine, k=None):
@@ -122,7 +131,7 @@ def test_matrix_repr_on_gpu(golden, engine):
         if engine == ENGINE_PLAIN:
             assert np.array_equal(got, want), case["cite"]
         else:
-            assert np.max(np.abs(got - want)) <= TOL, case["cite"]
+            assert_close(got, want)
 
 
 @pytest.mark.parametrize("engine", ENGINES)
@@ -138,7 +147,7 @@ def test_quantum_reg_vector(golden, engine):
     if engine == ENGINE_PLAIN:
         assert np.array_equal(got, want)
     else:
-        assert np.max(np.abs(got - want)) <= TOL
+        assert_close(got, want)
     mask = case["measure_mask"]
     for u in (0.0, 0.3, 0.77, 0.999):
         r = q.clone()
@@ -156,7 +165,7 @@ def test_random_all_kinds(n, engine):
     if engine == ENGINE_PLAIN:
         assert np.array_equal(got, want)
     else:
-        assert np.max(np.abs(got - want)) <= TOL
+        assert_close(got, want)
 
 
 @pytest.mark.parametrize("k", [6, 8, 10, 13])
@@ -165,7 +174,7 @@ def test_fused_widths(k):
     circ = all_kinds_circuit(n, 400, seed=77, ctrl_prob=0.5)
     want = run_oracle(n, 12345, circ)
     got = run_gpu(n, 12345, circ, ENGINE_FUSED, k=k).amplitudes()
-    assert np.max(np.abs(got - want)) <= TOL
+    assert_close(got, want)
 
 
 @pytest.mark.parametrize("engine", ENGINES)
@@ -178,7 +187,7 @@ def test_plain_circuit_20q(engine):
     if engine == ENGINE_PLAIN:
         assert np.array_equal(got, want)
     else:
-        assert np.max(np.abs(got - want)) <= TOL
+        assert_close(got, want)
     # measure_mask(0xFFFFF) with injected draws, against the oracle on the same state
     for u in (0.0, 0.123456789, 0.5, 0.987654321):
         r = q.clone()
@@ -202,7 +211,7 @@ def test_random_circuit_22q_plain_vs_oracle():
     got = run_gpu(22, 0, circ, ENGINE_PLAIN).amplitudes()
     assert np.array_equal(got, want)
     got_f = run_gpu(22, 0, circ, ENGINE_FUSED).amplitudes()
-    assert np.max(np.abs(got_f - want)) <= TOL
+    assert_close(got_f, want)
 
 
 def test_register_passes_vs_oracle():
@@ -324,7 +333,7 @@ def test_apply_host_plugin_matches_register():
     from qvnt_gb300 import default_context
     out = default_context().apply_host(circ, psi_i)
     want = run_oracle(n, 3, circ)
-    assert np.max(np.abs(out - want)) <= TOL
+    assert_close(out, want)
 
 
 def test_full_size_round_trip_30q():

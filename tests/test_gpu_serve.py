@@ -110,3 +110,39 @@ def test_serve_sheds_and_rejects():
     with pytest.raises(QvntError):
         s.submit(10, 0, None, [("measure", 1 << 12, 0.5)])  # mask outside the register
     s.close()
+
+
+def test_serve_wire_request_vs_oracle():
+    """A serving request received as a binary QVNW stream (gate records and calls, CRC-checked) is
+    decoded by Server.submit_request, run on the device, and matches the oracle driving qvnt's
+    QReg::with_state / apply / measure_mask (src/register/quant.rs:129-150, :376-395, :490-501) with
+    the same gates and draws: identical measured values, final amplitudes within 1e-12."""
+    import oracle_ref as orc
+    from qvnt_gb300 import op
+    from qvnt_gb300.circuits import random_circuit
+    from qvnt_gb300.serve import Server
+    from qvnt_gb300.wire import decode_request, encode_request
+
+    n, state = 12, 0b101100111010
+    ops = random_circuit(n, 3, seed=41, with_qft=False) * op.qft(0b111111) * op.h(0b1010).c(0b100000000)
+    cut = len(ops) // 2
+    calls = [("apply", cut), ("measure", 0b11, 0.61), ("apply", len(ops) - cut), ("measure", 0b1100000, 0.27)]
+    data = encode_request(n, state, ops, calls, keep_amplitudes=True)
+    assert decode_request(data)["calls"] == calls
+    s = Server(budget_bytes=1 << 30, slots=2)
+    rid = s.submit_request(data)
+    measured, amps, _ = s.wait(rid, timeout=60.0)
+    s.close()
+    gates = ops.gates()
+    psi = orc.new_state(n, state)
+    want, at = [], 0
+    for c in calls:
+        if c[0] == "apply":
+            orc.apply(gates[at:at + c[1]], psi)
+            at += c[1]
+            want.append(0)
+        else:
+            v, _ = orc.measure_mask(psi, n, c[1], c[2])
+            want.append(v)
+    assert [int(m) for m in measured] == want
+    assert np.max(np.abs(amps - psi)) <= TOL

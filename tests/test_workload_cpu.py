@@ -54,3 +54,18 @@ def test_precision_planner_terminates(n):
     p, b = ctypes.c_uint64(), ctypes.c_uint64()
     check(lib().qvnt_precision_plan_info(arr, cnt, n, ctypes.byref(p), ctypes.byref(b)))
     assert 0 < b.value <= cnt and 0 < p.value <= b.value
+
+
+@pytest.mark.parametrize("n,depth,seed", [(5, 3, 2), (24, 40, 2), (30, 40, 2)])
+def test_oracle_builders_give_the_same_circuit(n, depth, seed):
+    """The oracle-built workload (the CPU baseline's and the reference arm's circuit) is the
+    library-built one byte for byte, the config-2 shape included."""
+    import oracle_ref as orc
+    from qvnt_gb300.circuits import plain_circuit, random_circuit
+
+    a = [bytes(g) for g in random_circuit(n, depth, seed=seed).gates()]
+    b = [bytes(g) for g in orc.random_circuit_gates(n, depth, seed=seed)]
+    assert a == b
+    if n == 5:
+        a = [bytes(g) for g in plain_circuit(20, 20, seed=1).gates()]
+        assert a == [bytes(g) for g in orc.plain_circuit_gates(20, 20, seed=1)]

@@ -51,6 +51,29 @@ def test_norm_noalloc_matches_register_api():
         assert 0.0 < want < 1.0
 
 
+def test_norm_noalloc_ragged_lengths():
+    """Lengths that are not multiples of the 4096-amplitude chunk (a single partial chunk, a ragged
+    last chunk) against numpy's sum of |psi|^2, twice in a row."""
+    torch = pytest.importorskip("torch")
+    from qvnt_gb300 import _abi
+
+    lib = _abi.lib()
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(8)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for n_amps in (8, 17, 4095, 5000, 4096 * 3 + 17, 4096 * 37 + 1):
+        host = rng.normal(size=2 * n_amps)
+        want = float(np.sum(host * host))
+        d_psi = torch.from_numpy(host.copy()).to(dev)
+        d_out = torch.empty(1, dtype=torch.float64, device=dev)
+        for _ in range(2):
+            d_out.fill_(-1.0)
+            _sum_noalloc(lib, d_psi.data_ptr(), n_amps, d_out.data_ptr(), stream)
+            torch.cuda.synchronize(dev)
+            got = float(d_out.item())
+            assert abs(got - want) <= 1e-12 * want, (n_amps, got, want)
+
+
 def test_norm_noalloc_rejects_oversized_state():
     from qvnt_gb300 import _abi
 
