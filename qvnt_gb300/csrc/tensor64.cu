@@ -18,18 +18,26 @@
 // the result carries one rounding of the inputs (2^-53 of the row's power-of-two bound) and one
 // rounding to f64, no FP64 instruction is issued.
 //
-// Kernel (one pass = one block): persistent CTAs of 512 threads, one per SM (tensor memory: all
-// 512 columns).  Per tile of 4096 amplitudes (12 tile qubits: the 7 lowest, so a tile is 2 KB
-// runs, plus the block's): TMA bulk loads into one of two shared-memory buffers (the next tile
-// loads while this one computes); each thread takes one row (lane quadrant) and 8 of its 32
-// amplitudes, finds the row exponent with its three partners, slices its 16 reals and stores the
-// digits to two ping-pong operand slots in tensor memory; one thread issues each digit's MMAs and
-// commits them to the slot's mbarrier, so the next digit's store waits only for the digit two
-// before it.  Read-back, reconstruction and the TMA bulk store of the tile follow.
+// Kernel (one pass = one block): persistent CTAs, one per SM (tensor memory: all 512 columns), of
+// 18 warps (10 in the 16-amplitude layout) in three roles synchronised by mbarriers only.  Per tile of 4096 amplitudes (12 tile
+// qubits: the 7 lowest, so a tile is 2 KB runs, plus the block's):
+//   * the copy warp keeps two shared-memory tile buffers filled with TMA bulk loads and stores each
+//     tile once its results are written;
+//   * 16 math warps each take one operand row (lane quadrant) and 8 of its 32 amplitudes (or 8 warps
+//     and 16 amplitudes): the row exponent (with the row's other warps), the slices, and the digits stored one by one to
+//     two ping-pong operand slots in tensor memory (a slot takes digit s once the MMAs of digit s - 2
+//     are done); then the read-back of the seven levels and the rounding to f64;
+//   * the MMA warp issues each digit's products once its slot is full and commits them to the
+//     slot's mbarrier.
+// The next tile is sliced while this tile's last digits multiply, and this tile's results are
+// rounded while the next tile's first digits multiply: the tensor pipe waits only for the read-back
+// of the accumulators.
 #include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -53,7 +61,16 @@ using namespace tc;
 constexpr int kTQ = 12;                         // tile qubits
 constexpr uint32_t kTileAmps = 1u << kTQ;       // 4096 amplitudes, 64 KB
 constexpr uint32_t kLowQ = 7;                   // lowest qubits always in the tile (2 KB runs)
-constexpr uint32_t kNT = 512;                   // 16 warps: 4 lane quadrants x 4 column groups
+// Block layout for NA amplitudes per math thread (8 or 16): 4 lane quadrants x 32 / NA column
+// groups of math warps, then the MMA warp and the copy warp.
+template <int NA>
+struct Layout {
+    static constexpr uint32_t kCG = 32 / NA;             // column groups per row
+    static constexpr uint32_t kMathWarps = 4 * kCG;
+    static constexpr uint32_t kMmaWarp = kMathWarps;     // issues the MMAs
+    static constexpr uint32_t kTmaWarp = kMathWarps + 1; // issues the tile copies
+    static constexpr uint32_t kNT = 32 * (kMathWarps + 2);
+};
 constexpr int kDigits = 7;                      // base-256 digits per 53-bit operand
 constexpr uint32_t kWDigitBytes = 64 * 64 * 2;  // one fp16 digit matrix of a block (8 KB)
 constexpr uint32_t kWBlockBytes = kDigits * kWDigitBytes + 64 * 4;  // digits + 64 row exponents
@@ -104,57 +121,134 @@ __device__ __forceinline__ uint64_t slice(double x, uint32_t E) {
     return ((b >> 63) ? (0ull - v) : v) + kBias;
 }
 
-// Digits `byte` of two reals as a packed fp16 pair: fp16(1408 + c) has the bits 0x6580 + c for a
-// byte c, and subtracting 1536 leaves c - 128 exactly.
+// Digit byte `byte` of two reals as a packed fp16 pair: fp16(1408 + c) has the bits 0x6580 + c for
+// a byte c, and subtracting 1536 leaves c - 128 exactly.
 __device__ __forceinline__ uint32_t digit_pair(uint64_t y0, uint64_t y1, int byte) {
-    const uint32_t b0 = (uint32_t)(y0 >> (8 * byte)) & 0xffu;
-    const uint32_t b1 = (uint32_t)(y1 >> (8 * byte)) & 0xffu;
-    uint32_t h = (b0 | (b1 << 16)) + 0x65806580u;
+    const uint32_t w0 = byte < 4 ? (uint32_t)y0 : (uint32_t)(y0 >> 32);
+    const uint32_t w1 = byte < 4 ? (uint32_t)y1 : (uint32_t)(y1 >> 32);
+    const uint32_t j = (uint32_t)(byte & 3);
+    const uint32_t two = __byte_perm(w0, w1, j | ((4u + j) << 4));  // bytes (c0, c1, ., .)
+    uint32_t h = __byte_perm(two, 0u, 0x4140u) + 0x65806580u;        // (c0, 0, c1, 0) + bias
     __half2 v = *reinterpret_cast<__half2*>(&h);
     v = __hsub2(v, __halves2half2(__ushort_as_half((unsigned short)0x6600), __ushort_as_half((unsigned short)0x6600)));
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-// Integer value of an integer-valued float: |f| < 2^22 exactly; |f| < 2^23 to the nearest even
-// (f2i_even); round(f / 256).
-__device__ __forceinline__ int32_t f2i(float f) { return __float_as_int(f + 12582912.0f) - 0x4B400000; }
-__device__ __forceinline__ int32_t f2i_even(float f) { return (__float_as_int(f + 25165824.0f) - 0x4BC00000) * 2; }
-__device__ __forceinline__ int32_t f2i_div256(float f) {
-    return __float_as_int(fmaf(f, 0.00390625f, 12582912.0f)) - 0x4B400000;
-}
+// An integer-valued float as the bits of f + M, which hold the integer plus a constant: M = 1.5 * 2^23
+// (exact for |f| < 2^22, bits - 0x4B400000), M = 1.5 * 2^24 (|f| < 2^23 to the nearest even:
+// 2 (bits - 0x4BC00000)), and f / 256 + 1.5 * 2^23 (round(f / 256)).
+__device__ __forceinline__ uint32_t mbits(float f) { return __float_as_uint(f + 12582912.0f); }
+__device__ __forceinline__ uint32_t mbits_even(float f) { return __float_as_uint(f + 25165824.0f); }
+__device__ __forceinline__ uint32_t mbits_div256(float f) { return __float_as_uint(fmaf(f, 0.00390625f, 12582912.0f)); }
+// The constants those bits carry, summed with the level weights 2^(8 (5 - l)) (levels 0..4 and 6:
+// 0x4B400000; level 5, counted twice: 0x4BC00000), modulo 2^64.
+constexpr uint64_t kMagicSum = 0x4B400000ull * ((1ull << 40) + (1ull << 32) + (1ull << 24) + (1ull << 16) + (1ull << 8) + 1ull) +
+                               2ull * 0x4BC00000ull;
 
 // v * 2^T rounded to the nearest f64 (ties to even); below the normal range: signed zero.
 __device__ __forceinline__ double scaled_to_f64(int64_t v, int T) {
-    if (v == 0) return 0.0;
     const uint64_t sgn = (uint64_t)v & 0x8000000000000000ull;
-    uint64_t a = v < 0 ? 0ull - (uint64_t)v : (uint64_t)v;
+    const uint64_t a = (uint64_t)((v ^ (v >> 63)) - (v >> 63));  // |v|
+    if (a == 0) return 0.0;
     const int lz = __clzll((long long)a);
-    a <<= lz;
-    uint64_t mant = a >> 11;
-    const uint32_t rem = (uint32_t)a & 0x7ffu;
-    mant += (uint64_t)((rem > 0x400u) | ((rem == 0x400u) & (uint32_t)(mant & 1ull)));
-    const int e = 63 - lz + T + 1023;
+    const uint64_t n = a << lz;                        // leading one at bit 63
+    uint64_t mant = n >> 11;                           // 53 bits
+    const uint32_t low = (uint32_t)n & 0x7ffu;         // round bit 10, sticky bits 0..9
+    mant += (low >> 10) & ((low & 0x3ffu) != 0u | (uint32_t)mant) & 1u;
+    const int e = 1086 - lz + T;                       // biased exponent of a * 2^T
     if (e <= 0) return __longlong_as_double((long long)sgn);
     return __longlong_as_double((long long)(sgn | (((uint64_t)(e - 1) << 52) + mant)));
 }
 
-__global__ void __launch_bounds__(kNT, 1)
+// A wait that sleeps in hardware until the phase completes, in slices of kSleepNs; it gives up
+// after kSleepSlices slices (about two seconds; setting the error flag and the block's abort flag)
+// or as soon as another role has aborted.
+constexpr uint32_t kSleepNs = 1000000;
+constexpr uint32_t kSleepSlices = 2000;
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                              int* err) {
+    for (uint32_t it = 0; it < kSleepSlices; ++it) {
+        if (mbar_try_sleep(bar, parity, kSleepNs)) return true;
+        if (*abort_flag) return false;
+    }
+    atomicExch(err, 1);
+    *abort_flag = 1;
+    return false;
+}
+
+// Digit S (0 = most significant) of the thread's 2 NA reals into an operand slot, then one arrival
+// per warp on the slot's "full" barrier.
+template <int S, int NA>
+__device__ __forceinline__ void put_digit(const uint64_t (&y)[2 * NA], uint32_t tmem_slot_addr, uint64_t* full,
+                                          uint32_t lane) {
+    uint32_t v[NA];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) v[i] = digit_pair(y[2 * i], y[2 * i + 1], 6 - S);
+    if constexpr (NA == 16) tmem_st16(tmem_slot_addr, v);
+    else tmem_st8(tmem_slot_addr, v);
+    tmem_st_wait();
+    tc_before_sync();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(full);
+}
+
+// Math warps: the tile in buffer b once loaded, its row exponent E (with the row's other column
+// groups, through s_exp and the quad's named barrier) and the thread's 2 NA slices y.
+template <int NA>
+__device__ __forceinline__ bool prep_tile(const double2* tiles, uint32_t b, uint32_t& ph_tma, uint32_t mrow,
+                                          const uint32_t* rp, uint32_t (*s_exp)[32 / NA][128], uint32_t cg,
+                                          uint32_t quad, uint32_t row, uint64_t (&y)[2 * NA], uint32_t& E,
+                                          volatile int* abort_flag, int* err, uint64_t* bar_tma, uint32_t* loads_seen) {
+    constexpr uint32_t kCG = 32 / NA;
+    if (!wait_or_abort(&bar_tma[b], (ph_tma >> b) & 1u, abort_flag, err)) return false;
+    ph_tma ^= 1u << b;
+    if (loads_seen) ++loads_seen[b];
+    const double2* tile = tiles + (size_t)b * kTileAmps;
+    uint32_t emax = 0;
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {  // first read: the row exponent
+        const double2 a = tile[mrow | rp[i]];
+        const uint32_t e0 = (uint32_t)((uint64_t)__double_as_longlong(a.x) >> 52) & 0x7ffu;
+        const uint32_t e1 = (uint32_t)((uint64_t)__double_as_longlong(a.y) >> 52) & 0x7ffu;
+        emax = max(emax, max(e0, e1));
+    }
+    s_exp[b][cg][row] = emax;
+    named_sync(1u + quad, 32u * kCG);
+    E = s_exp[b][0][row];
+#pragma unroll
+    for (uint32_t g = 1; g < kCG; ++g) E = max(E, s_exp[b][g][row]);
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {  // second read: the slices
+        const double2 a = tile[mrow | rp[i]];
+        y[2 * i] = slice(a.x, E);
+        y[2 * i + 1] = slice(a.y, E);
+    }
+    return true;
+}
+
+template <int kRegs, int NA>
+__global__ void __maxnreg__(kRegs)
     tensor64_pass_kernel(double2* __restrict__ psi, const unsigned char* __restrict__ wts,
                          const __grid_constant__ TPassParams P, int* __restrict__ err) {
+    using LY = Layout<NA>;
+    constexpr uint32_t kNT = LY::kNT, kMathWarps = LY::kMathWarps, kMmaWarp = LY::kMmaWarp, kTmaWarp = LY::kTmaWarp;
+    constexpr uint32_t kCG = LY::kCG;
     extern __shared__ __align__(1024) unsigned char smem[];
     double2* tiles = reinterpret_cast<double2*>(smem);  // two tile buffers
     unsigned char* w_sm = smem + 2 * (size_t)kTileAmps * 16;
     __shared__ uint64_t seg_off[1u << (kTQ - kLowQ)];
     __shared__ uint32_t mpos[128];
     __shared__ uint32_t rpos[32];
-    __shared__ uint32_t s_exp[4][128];
-    __shared__ __align__(8) uint64_t bar_tma[2];
-    __shared__ __align__(8) uint64_t bar_mma[2];
+    __shared__ uint32_t s_exp[2][kCG][128];
+    __shared__ __align__(8) uint64_t bar_tma[2];      // tile loaded into buffer b (TMA bytes)
+    __shared__ __align__(8) uint64_t bar_written[2];  // tile results written to buffer b (16 math warps)
+    __shared__ __align__(8) uint64_t bar_full[2];     // operand slot holds the next digit (16 math warps)
+    __shared__ __align__(8) uint64_t bar_mma[2];      // that digit's MMAs are done (commit)
+    __shared__ __align__(8) uint64_t bar_acc;         // accumulators read back (16 math warps)
     __shared__ uint32_t tmem_base;
     __shared__ int s_abort;
+    __shared__ uint32_t s_loads[2], s_loads_seen[2], s_commits[2], s_commits_seen[2];
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t quad = warp & 3u, cg = warp >> 2;
-    const uint32_t row = 32u * quad + lane;  // operand row (lane of tensor memory)
     const uint32_t c = P.c;
     const uint32_t nseg = 1u << (kTQ - c);
     const uint32_t seg_amps = 1u << c;
@@ -194,8 +288,12 @@ __global__ void __launch_bounds__(kNT, 1)
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
             mbar_init(&bar_tma[i], 1);
+            mbar_init(&bar_written[i], kMathWarps);
+            mbar_init(&bar_full[i], kMathWarps);
             mbar_init(&bar_mma[i], 1);
+            s_loads[i] = s_loads_seen[i] = s_commits[i] = s_commits_seen[i] = 0;
         }
+        mbar_init(&bar_acc, kMathWarps);
         s_abort = 0;
         fence_mbar_init();
     }
@@ -204,14 +302,9 @@ __global__ void __launch_bounds__(kNT, 1)
     __syncthreads();
     tc_after_sync();
     const uint32_t tmem = tmem_base;
-    const uint32_t lane_addr = (32u * quad) << 16;
-    const int32_t* w_exp = reinterpret_cast<const int32_t*>(w_sm + kDigits * kWDigitBytes);
-    int32_t fexp[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) fexp[i] = w_exp[16 * cg + i];
-    const uint32_t w_addr = smem_addr(w_sm);
-    const bool leader = warp == 0;
-    uint32_t ph_tma[2] = {0, 0}, ph_mma[2] = {0, 0};
+    volatile int* abort_flag = &s_abort;
+    const uint64_t first = blockIdx.x, stride = gridDim.x;
+    const uint32_t my_tiles = first < P.ntiles ? (uint32_t)((P.ntiles - 1 - first) / stride + 1) : 0u;
 
     auto tile_base = [&](uint64_t t) {
         uint64_t base = t;
@@ -221,137 +314,172 @@ __global__ void __launch_bounds__(kNT, 1)
         }
         return base;
     };
-    auto issue_load = [&](uint64_t t, uint32_t b) {  // leader warp
-        const uint64_t base = tile_base(t);
-        double2* dst = tiles + (size_t)b * kTileAmps;
-        if (lane == 0) {
-            fence_proxy_async();
-            mbar_expect_tx(&bar_tma[b], kTileAmps * 16u);
-        }
-        __syncwarp();
-        for (uint32_t s = lane; s < nseg; s += 32)
-            bulk_load(dst + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 16u, &bar_tma[b]);
-    };
-    auto wait_bar = [&](uint64_t* bar, uint32_t& ph) {
-        if (!mbar_wait(bar, ph, kWaitLimit)) {
-            atomicExch(err, 1);
-            s_abort = 1;
-        }
-        ph ^= 1u;
-    };
 
-    if (leader && (uint64_t)blockIdx.x < P.ntiles) issue_load(blockIdx.x, 0);
-    uint32_t it = 0;
-    for (uint64_t t = blockIdx.x; t < P.ntiles; t += gridDim.x, ++it) {
-        const uint32_t b = it & 1u;
-        double2* tile = tiles + (size_t)b * kTileAmps;
-        wait_bar(&bar_tma[b], ph_tma[b]);
-        // this thread's 8 amplitudes of its row, and the row exponent
-        uint32_t pos[8];
-        double2 a[8];
-        uint32_t emax = 0;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            pos[i] = mpos[row] | rpos[8u * cg + i];
-            a[i] = tile[pos[i]];
-            const uint32_t e0 = (uint32_t)((uint64_t)__double_as_longlong(a[i].x) >> 52) & 0x7ffu;
-            const uint32_t e1 = (uint32_t)((uint64_t)__double_as_longlong(a[i].y) >> 52) & 0x7ffu;
-            emax = max(emax, max(e0, e1));
-        }
-        s_exp[cg][row] = emax;
-        __syncthreads();
-        if (s_abort) break;
-        const uint32_t E = max(max(s_exp[0][row], s_exp[1][row]), max(s_exp[2][row], s_exp[3][row]));
-        // the next tile loads into the other buffer once its last store has read it
-        const uint64_t tn = t + gridDim.x;
-        if (leader && tn < P.ntiles) {
-            bulk_wait_read();
-            issue_load(tn, b ^ 1u);
-        }
-        uint64_t y[16];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            y[2 * i] = slice(a[i].x, E);
-            y[2 * i + 1] = slice(a[i].y, E);
-        }
-        // digits, most significant first, through the two operand slots
-#pragma unroll
-        for (int s = 0; s < kDigits; ++s) {
-            const uint32_t slot = (uint32_t)s & 1u;
-            if (s >= 2) {
-                wait_bar(&bar_mma[slot], ph_mma[slot]);
-                tc_after_sync();
+    if (warp == kTmaWarp) {
+        // ---- copies: loads two tiles ahead of the math warps, stores each tile once written ----
+        auto issue_load = [&](uint32_t i) {
+            const uint32_t b = i & 1u;
+            const uint64_t base = tile_base(first + i * stride);
+            double2* dst = tiles + (size_t)b * kTileAmps;
+            if (lane == 0) {
+                ++s_loads[b];
+                mbar_expect_tx(&bar_tma[b], kTileAmps * 16u);
             }
-            uint32_t v[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) v[i] = digit_pair(y[2 * i], y[2 * i + 1], 6 - s);
-            tmem_st8(tmem + lane_addr + kSlotCol + 32u * slot + 8u * cg, v);
-            tmem_st_wait();
-            tc_before_sync();
-            __syncthreads();
-            if (tid == 0 && !s_abort) {
-                tc_after_sync();
-                const uint32_t a_tm = tmem + kSlotCol + 32u * slot;
-                for (int tt = 0; tt + s < kDigits; ++tt) {
-                    const uint32_t d_tm = tmem + 64u * (uint32_t)(s + tt);
-                    const uint32_t wb = w_addr + (uint32_t)tt * kWDigitBytes;
-#pragma unroll
-                    for (uint32_t ks = 0; ks < 4; ++ks)
-                        mma_f16_ta(d_tm, a_tm + 8u * ks, smem_desc(wb + 256u * ks, 128u, 1024u),
-                                   (s > 0 || ks > 0) ? 1u : 0u);
-                }
-                mma_commit(&bar_mma[slot]);
-            }
-        }
-        // all 28 digit products done (the last commit of each slot)
-        wait_bar(&bar_mma[0], ph_mma[0]);
-        wait_bar(&bar_mma[1], ph_mma[1]);
-        tc_after_sync();
-        // read back the seven levels of this thread's 16 output reals and round them to f64
-        int32_t hi[16];
-        int64_t acc[16];
-#pragma unroll
-        for (int l = 0; l < kDigits; ++l) {
-            uint32_t v[16];
-            tmem_ld16(tmem + lane_addr + 64u * (uint32_t)l + 16u * cg, v);
-            tmem_ld_wait();
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const float f = __uint_as_float(v[i]);
-                if (l == 0) hi[i] = f2i(f);
-                else if (l == 1) hi[i] = hi[i] * 256 + f2i(f);
-                else if (l == 2) acc[i] = (int64_t)f2i(f) << 24;
-                else if (l == 3) acc[i] += (int64_t)f2i(f) << 16;
-                else if (l == 4) acc[i] += (int64_t)f2i(f) << 8;
-                else if (l == 5) acc[i] += (int64_t)f2i_even(f);
-                else acc[i] += (int64_t)f2i_div256(f);
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int64_t v0 = acc[2 * i] + ((int64_t)hi[2 * i] << 32);
-            const int64_t v1 = acc[2 * i + 1] + ((int64_t)hi[2 * i + 1] << 32);
-            tile[pos[i]] = make_double2(scaled_to_f64(v0, (int)E + fexp[2 * i] - 2094),
-                                        scaled_to_f64(v1, (int)E + fexp[2 * i + 1] - 2094));
-        }
-        tc_before_sync();
-        fence_proxy_async();
-        __syncthreads();
-        if (s_abort) break;
-        if (leader) {
-            const uint64_t base = tile_base(t);
+            __syncwarp();
             for (uint32_t s = lane; s < nseg; s += 32)
-                bulk_store(psi + (base | seg_off[s]), tile + (size_t)s * seg_amps, seg_amps * 16u);
+                bulk_load(dst + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 16u, &bar_tma[b]);
+        };
+        uint32_t ph_w = 0;  // phase parity of bar_written[b] in bit b
+        for (uint32_t i = 0; i < my_tiles && i < 2; ++i) issue_load(i);
+        for (uint32_t i = 0; i < my_tiles; ++i) {
+            const uint32_t b = i & 1u;
+            if (!wait_or_abort(&bar_written[b], (ph_w >> b) & 1u, abort_flag, err)) break;
+            ph_w ^= 1u << b;
+            const uint64_t base = tile_base(first + i * stride);
+            const double2* src = tiles + (size_t)b * kTileAmps;
+            for (uint32_t s = lane; s < nseg; s += 32)
+                bulk_store(psi + (base | seg_off[s]), src + (size_t)s * seg_amps, seg_amps * 16u);
             bulk_commit();
+            bulk_wait_read();  // the buffer is free for the tile two ahead
+            __syncwarp();
+            if (i + 2 < my_tiles) issue_load(i + 2);
+        }
+        bulk_wait_all();
+    } else if (warp == kMmaWarp) {
+        // ---- MMA issue: digit s of a tile once its slot is full (and, for digit 0, once the
+        // previous tile's accumulators have been read back) ----
+        const uint32_t w_addr = smem_addr(w_sm);
+        uint32_t ph_full = 0, ph_acc = 0;  // phase parities, bit = slot
+        bool ok = true;
+        for (uint32_t i = 0; ok && i < my_tiles; ++i) {
+#pragma unroll
+            for (int s = 0; s < kDigits; ++s) {
+                const uint32_t slot = (uint32_t)s & 1u;
+                if (ok && s == 0 && i > 0) {
+                    ok = wait_or_abort(&bar_acc, ph_acc, abort_flag, err);
+                    ph_acc ^= 1u;
+                }
+                if (ok) ok = wait_or_abort(&bar_full[slot], (ph_full >> slot) & 1u, abort_flag, err);
+                ph_full ^= 1u << slot;
+                if (ok && lane == 0) {
+                    tc_after_sync();
+                    const uint32_t a_tm = tmem + kSlotCol + 32u * slot;
+#pragma unroll
+                    for (int tt = 0; tt + s < kDigits; ++tt) {
+                        const uint32_t d_tm = tmem + 64u * (uint32_t)(s + tt);
+                        const uint32_t wb = w_addr + (uint32_t)tt * kWDigitBytes;
+#pragma unroll
+                        for (uint32_t ks = 0; ks < 4; ++ks)
+                            mma_f16_ta(d_tm, a_tm + 8u * ks, smem_desc(wb + 256u * ks, 128u, 1024u),
+                                       (s > 0 || ks > 0) ? 1u : 0u);
+                    }
+                    mma_commit(&bar_mma[slot]);
+                    ++s_commits[slot];
+                }
+                __syncwarp();
+            }
+        }
+    } else {
+        // ---- math warps: a row (lane quadrant) and NA of its 32 amplitudes (column group) ----
+        const uint32_t quad = warp & 3u, cg = warp >> 2;
+        const uint32_t row = 32u * quad + lane;
+        const uint32_t lane_addr = (32u * quad) << 16;
+        const uint32_t slot0 = tmem + lane_addr + kSlotCol + (uint32_t)NA * cg;
+        const int32_t* w_exp = reinterpret_cast<const int32_t*>(w_sm + kDigits * kWDigitBytes) + 2u * NA * cg;
+        const uint32_t* rp = rpos + (uint32_t)NA * cg;
+        const uint32_t mrow = mpos[row];  // amplitude i of this thread sits at mrow | rp[i]
+        const bool counter = quad == 0 && cg == 0 && lane == 0;
+        uint32_t ph_tma = 0, ph_mma = 0;  // phase parities, bit = buffer / slot
+        uint64_t y[2 * NA];
+        uint32_t E = 0;
+        auto wait_mma = [&](uint32_t slot) -> bool {
+            const bool r = wait_or_abort(&bar_mma[slot], (ph_mma >> slot) & 1u, abort_flag, err);
+            ph_mma ^= 1u << slot;
+            if (r && counter) ++s_commits_seen[slot];
+            tc_after_sync();
+            return r;
+        };
+        bool ok = my_tiles > 0 && prep_tile<NA>(tiles, 0, ph_tma, mrow, rp, s_exp, cg, quad, row, y, E, abort_flag, err,
+                                            bar_tma, counter ? s_loads_seen : nullptr);
+        if (ok) {
+            put_digit<0, NA>(y, slot0, &bar_full[0], lane);
+            put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
+        }
+        for (uint32_t i = 0; ok && i < my_tiles; ++i) {
+            const uint32_t b = i & 1u;
+            // a slot takes digit s once the MMAs of digit s - 2 are done
+            ok = wait_mma(0);
+            if (ok) put_digit<2, NA>(y, slot0, &bar_full[0], lane);
+            if (ok) ok = wait_mma(1);
+            if (ok) put_digit<3, NA>(y, slot0 + 32u, &bar_full[1], lane);
+            if (ok) ok = wait_mma(0);
+            if (ok) put_digit<4, NA>(y, slot0, &bar_full[0], lane);
+            if (ok) ok = wait_mma(1);
+            if (ok) put_digit<5, NA>(y, slot0 + 32u, &bar_full[1], lane);
+            if (ok) ok = wait_mma(0);
+            if (ok) put_digit<6, NA>(y, slot0, &bar_full[0], lane);
+            if (!ok) break;
+            // the next tile's slices while this tile's last digits multiply
+            const uint32_t E_this = E;
+            const bool has_next = i + 1 < my_tiles;
+            if (has_next)
+                ok = prep_tile<NA>(tiles, b ^ 1u, ph_tma, mrow, rp, s_exp, cg, quad, row, y, E, abort_flag, err, bar_tma,
+                               counter ? s_loads_seen : nullptr);
+            // every MMA of this tile done: the commits of digits 6 (slot 0) and 5 (slot 1)
+            const bool done0 = wait_mma(0);
+            const bool done1 = wait_mma(1);
+            if (!(done0 && done1)) break;
+            // the seven levels of this thread's 2 NA output reals: sum of level x 2^(8 (5 - l)), from the
+            // magic-number bits (their constants removed at the end, modulo 2^64)
+            uint64_t acc[2 * NA];
+#pragma unroll
+            for (int l = 0; l < kDigits; ++l) {
+#pragma unroll
+                for (int part = 0; part < NA / 4; ++part) {
+                    uint32_t v[8];
+                    tmem_ld8(tmem + lane_addr + 64u * (uint32_t)l + 2u * NA * cg + 8u * (uint32_t)part, v);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int kk = 0; kk < 8; ++kk) {
+                        const int k = 8 * part + kk;
+                        const float f = __uint_as_float(v[kk]);
+                        if (l == 0) acc[k] = (uint64_t)mbits(f) << 32;
+                        else if (l == 1) acc[k] = (uint64_t)((uint32_t)(acc[k] >> 32) * 256u + mbits(f)) << 32;
+                        else if (l < 5) acc[k] += (uint64_t)mbits(f) << (8 * (5 - l));
+                        else if (l == 5) acc[k] += 2ull * mbits_even(f);
+                        else acc[k] += mbits_div256(f);
+                    }
+                }
+            }
+            tc_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_acc);
+            // the next tile's first two digits go in while this tile's results are rounded
+            if (has_next && ok) {
+                put_digit<0, NA>(y, slot0, &bar_full[0], lane);
+                put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
+            }
+            double2* tile = tiles + (size_t)b * kTileAmps;
+#pragma unroll
+            for (int k = 0; k < NA; ++k)
+                tile[mrow | rp[k]] =
+                    make_double2(scaled_to_f64((int64_t)(acc[2 * k] - kMagicSum), (int)E_this + w_exp[2 * k] - 2094),
+                                 scaled_to_f64((int64_t)(acc[2 * k + 1] - kMagicSum), (int)E_this + w_exp[2 * k + 1] - 2094));
+            fence_proxy_async();  // the results are read by the TMA store
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_written[b]);
         }
     }
-    if (s_abort) {  // let the copies and MMAs in flight finish before the memory goes away
-        mbar_wait(&bar_tma[0], ph_tma[0], kWaitLimit);
-        mbar_wait(&bar_tma[1], ph_tma[1], kWaitLimit);
-        mbar_wait(&bar_mma[0], ph_mma[0], kWaitLimit);
-        mbar_wait(&bar_mma[1], ph_mma[1], kWaitLimit);
+    // teardown: after an abort, let the copies and MMAs in flight land before the memory goes away
+    __syncthreads();
+    if (s_abort && tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            uint32_t seen = s_loads_seen[b];
+            while (seen < s_loads[b] && mbar_wait(&bar_tma[b], seen & 1u, kWaitLimit)) ++seen;
+            seen = s_commits_seen[b];
+            while (seen < s_commits[b] && mbar_wait(&bar_mma[b], seen & 1u, kWaitLimit)) ++seen;
+        }
     }
-    if (leader) bulk_wait_all();
     tc_before_sync();
     __syncthreads();
     tc_after_sync();
@@ -427,6 +555,53 @@ int plan_blocks(const qvnt_gate* gates, size_t count, uint32_t L, std::vector<de
     return dense::make_passes(blocks, L, kTQ, kLowQ, 1, passes);
 }
 
+using PassFn = void (*)(double2*, const unsigned char*, const TPassParams, int*);
+struct PassKernel {
+    PassFn fn = nullptr;
+    uint32_t threads = 0;
+    int regs = 0;
+    char why[160] = {0};
+};
+
+// The kernel builds in order of preference (measured on a 30-qubit pass: 17.1 ms against 20.3 ms):
+// 16 math warps of 8 amplitudes with 96 registers (five of the eighteen warps share an SM
+// sub-partition's 16K registers), 8 math warps of 16 amplitudes with 168 registers (three of ten);
+// QVNT_T64_LAYOUT=8 or 16 picks one (amplitudes per math thread).
+PassKernel pick_kernel() {
+    PassKernel k;
+    struct Cand {
+        PassFn fn;
+        uint32_t threads;
+        int na;
+    };
+    const Cand cands[3] = {{tensor64_pass_kernel<96, 8>, Layout<8>::kNT, 8},
+                           {tensor64_pass_kernel<168, 16>, Layout<16>::kNT, 16},
+                           {tensor64_pass_kernel<128, 16>, Layout<16>::kNT, 16}};
+    const char* env = std::getenv("QVNT_T64_LAYOUT");
+    const int want = env ? std::atoi(env) : 0;
+    for (const Cand& c : cands) {
+        if (want && c.na != want) continue;
+        cudaFuncAttributes a;
+        if (cudaFuncGetAttributes(&a, (const void*)c.fn) != cudaSuccess) continue;
+        if (a.maxThreadsPerBlock < (int)c.threads) {
+            snprintf(k.why, sizeof k.why, "%d registers allow %d threads per block, %u needed", a.numRegs,
+                     a.maxThreadsPerBlock, c.threads);
+            continue;
+        }
+        if (cudaFuncSetAttribute((const void*)c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDyn) !=
+            cudaSuccess) {
+            snprintf(k.why, sizeof k.why, "shared-memory attribute refused");
+            continue;
+        }
+        k.fn = c.fn;
+        k.threads = c.threads;
+        k.regs = a.numRegs;
+        return k;
+    }
+    cudaGetLastError();
+    return k;
+}
+
 int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
     std::vector<dense::Block> blocks;
@@ -445,11 +620,8 @@ int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     unsigned char* hw = static_cast<unsigned char*>(fs.h_buf);
     for (size_t i = 0; i < blocks.size(); ++i) block_weights64(blocks[i], hw + i * (size_t)kWBlockBytes);
     QVNT_CUDA_TRY(cudaMemcpyAsync(fs.d_buf, fs.h_buf, wbytes, cudaMemcpyHostToDevice, r->stream));
-    static const bool attr = [] {
-        return cudaFuncSetAttribute((const void*)tensor64_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kSmemDyn) == cudaSuccess;
-    }();
-    if (!attr) return set_error(QVNT_ERR_CUDA, "tensor64 kernel: shared-memory attribute refused");
+    static const PassKernel kern = pick_kernel();
+    if (!kern.fn) return set_error(QVNT_ERR_CUDA, "tensor64 kernel: %s", kern.why);
     int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
     for (const dense::PPlan& p : passes) {
         TPassParams P;
@@ -475,9 +647,12 @@ int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
         const uint64_t grid = std::min<uint64_t>((uint64_t)r->ctx->geo.sms, P.ntiles);
         cudaEvent_t stop = nullptr;
         TRY_T(timing_begin(r, &stop));
-        tensor64_pass_kernel<<<(unsigned)grid, kNT, kSmemDyn, r->stream>>>(
-            r->psi, static_cast<const unsigned char*>(fs.d_buf), P, d_err);
-        QVNT_CUDA_TRY(cudaGetLastError());
+        kern.fn<<<(unsigned)grid, kern.threads, kSmemDyn, r->stream>>>(r->psi, static_cast<const unsigned char*>(fs.d_buf), P,
+                                                               d_err);
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess)
+            return set_error(QVNT_ERR_CUDA, "tensor64 launch (%d threads, %zu B dynamic shared memory, %d registers): %s",
+                             (int)kern.threads, kSmemDyn, kern.regs, cudaGetErrorString(le));
         TRY_T(timing_end(r, stop));
         r->launches += 1;
         r->passes += 1;
