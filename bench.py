@@ -77,6 +77,10 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--cpu-per-class", type=int, default=3, help="gates per stratum in the cpu_baseline sample")
+    ap.add_argument("--precision-qubits", type=int, default=32)
+    ap.add_argument("--precision-depth", type=int, default=60)
+    ap.add_argument("--precision-ref-qubits", type=int, default=30, help="size of the fidelity check (0 = none)")
+    ap.add_argument("--batch-fusion", default="auto", help="batch form: 'auto' (autotune) or 'K,BUDGET'")
     return ap.parse_args()
 
 
@@ -233,7 +237,7 @@ class CpuSampler:
         return len(self.gates) / est, self.threads, desc
 
 
-def bench_batch(ctx, count, steps):
+def bench_batch(ctx, count, steps, fusion="auto"):
     """Batching form: `count` registers (n uniform in [8, 20], depth uniform in [10, 60], random basis
     state, measure_mask of all qubits) in one persistent launch per run, tile width and pass budget
     autotuned on every 16th register.  Beside it, the plain f64 GPU path (one register at a time,
@@ -245,7 +249,12 @@ def bench_batch(ctx, count, steps):
 
     w = batch_workload(count=count)
     b = Batch(w.q_nums, w.states, w.gates, w.offsets, w.masks, ctx=ctx)
-    k, budget, tune_ms = b.autotune(stride=16)
+    if fusion == "auto":
+        k, budget, tune_ms = b.autotune(stride=16)
+    else:
+        k, budget = (int(x) for x in fusion.split(","))
+        b.set_fusion(k, budget)
+        tune_ms = None
     rng = SplitMix64(17)
     u01 = np.array([rng.uniform() for _ in range(w.count)])
     b.run(u01)  # warm-up
@@ -331,14 +340,16 @@ def bench_precision(ctx, n=32, depth=60, n_ref=30):
     qp.close()
     del qp
     # fidelity at n_ref qubits against IEEE f64 (the plain engine, bit-identical to the oracle)
-    arr_r, cnt_r = gates(n_ref)
-    a = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_PRECISION)
-    a.apply_gates(arr_r, cnt_r)
-    b = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_PLAIN)
-    b.apply_gates(arr_r, cnt_r)
-    fid, mx = a.overlap(b)
-    a.close()
-    b.close()
+    fid, mx, cnt_r = float("nan"), float("nan"), 0
+    if n_ref:
+        arr_r, cnt_r = gates(n_ref)
+        a = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_PRECISION)
+        a.apply_gates(arr_r, cnt_r)
+        b = QReg(n_ref, 0, ctx=ctx, engine=ENGINE_PLAIN)
+        b.apply_gates(arr_r, cnt_r)
+        fid, mx = a.overlap(b)
+        a.close()
+        b.close()
     avg = kms / kn
     return {"workload": "%d qubits complex<f32>, random layers depth %d (%d gates), dense 5-qubit blocks on tcgen05 "
                         "(TF32 hi/lo, FP32 accumulate), FP64 norm restoration every 10 passes" % (n, depth, cnt),
@@ -601,14 +612,15 @@ def main():
                     if engine != ENGINE_FUSED:
                         forms["df64"] = bench_df64(ctx, garr, ngates, n, max(1, min(args.steps, 3)))
                 elif form == "batch":
-                    forms["batch"] = bench_batch(ctx, args.batch_count, max(1, min(args.steps, 5)))
+                    forms["batch"] = bench_batch(ctx, args.batch_count, max(1, min(args.steps, 5)), args.batch_fusion)
                 elif form == "serve":
                     forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds)
                     # the same request mix at a rate one GPU sustains (the configured rate is about
                     # two orders of magnitude above its capacity for this mix)
                     forms["serve"]["at_sustainable_rate"] = bench_serve(ctx, 4.0, min(args.serve_seconds, 20.0))
                 elif form == "precision":
-                    forms["precision"] = bench_precision(ctx)
+                    forms["precision"] = bench_precision(ctx, args.precision_qubits, args.precision_depth,
+                                                         args.precision_ref_qubits)
             except Exception as exc:  # a form's failure is reported, not hidden
                 forms[form] = {"error": "%s: %s" % (type(exc).__name__, exc)}
 
