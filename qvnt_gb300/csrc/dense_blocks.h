@@ -36,6 +36,7 @@ inline uint64_t compress(uint64_t x, const std::vector<int>& sup) {  // global m
 struct LGate {
     uint64_t sup = 0;     // global support mask (<= 5 bits)
     std::vector<Cd> m;    // dense matrix over the support's local basis, row-major
+    bool diag = false;    // m is diagonal (such gates commute with each other)
 };
 
 // The dense matrix of one gate on its support, from qvnt's own atomic formulas (atomic.cuh) and the
@@ -66,6 +67,13 @@ inline int dense_gate(const qvnt_gate& g, LGate& out) {
             out.m[r * dim + cidx] = Cd{v.x, v.y};
         }
     }
+    out.diag = true;
+    for (uint64_t r = 0; r < dim && out.diag; ++r)
+        for (uint64_t cidx = 0; cidx < dim; ++cidx)
+            if (r != cidx && (out.m[r * dim + cidx].re != 0.0 || out.m[r * dim + cidx].im != 0.0)) {
+                out.diag = false;
+                break;
+            }
     return QVNT_OK;
 }
 
@@ -135,7 +143,35 @@ inline void block_apply(Block& b, const LGate& g) {
         }
 }
 
+// One candidate block seeded by gate `seed` (its support starts the block's qubit set): scanning the
+// unplaced gates in order from `first`, a gate joins when its support fits the five qubits and it
+// commutes with each gate skipped so far (their supports are disjoint, or both are diagonal).  Empty
+// when the seed itself cannot join (it does not commute with a gate skipped before it).
+inline std::vector<size_t> block_trial(const std::vector<LGate>& lg, const std::vector<char>& done, size_t first,
+                                       size_t seed, uint64_t all) {
+    std::vector<size_t> members;
+    uint64_t S = lg[seed].sup, skipped_nd = 0, skipped_d = 0;  // skipped supports: non-diagonal, diagonal
+    size_t scanned = 0;
+    for (size_t j = first; j < lg.size() && scanned < 512; ++j) {
+        if (done[j]) continue;
+        ++scanned;
+        const uint64_t G = lg[j].sup;
+        const uint64_t must_miss = lg[j].diag ? skipped_nd : (skipped_nd | skipped_d);
+        if (!(G & must_miss) && __builtin_popcountll(S | G) <= kBQ) {
+            S |= G;
+            members.push_back(j);
+        } else {
+            if (j == seed) return {};
+            (lg[j].diag ? skipped_d : skipped_nd) |= G;
+            if ((skipped_nd & all) == all && j > seed) break;  // nothing later can pass the skipped gates
+        }
+    }
+    return members;
+}
+
+// Blocks: each is the largest of the candidate blocks seeded by the first kSeeds unplaced gates.
 inline void make_blocks(const std::vector<LGate>& lg, uint32_t L, std::vector<Block>& blocks) {
+    constexpr size_t kSeeds = 48;
     blocks.clear();
     const size_t n = lg.size();
     std::vector<char> done(n, 0);
@@ -144,21 +180,18 @@ inline void make_blocks(const std::vector<LGate>& lg, uint32_t L, std::vector<Bl
     while (true) {
         while (first < n && done[first]) ++first;
         if (first >= n) break;
-        uint64_t S = 0, blocked = 0;
         std::vector<size_t> members;
-        size_t scanned = 0;
-        for (size_t j = first; j < n && scanned < 512; ++j) {
-            if (done[j]) continue;
-            ++scanned;
-            const uint64_t G = lg[j].sup;
-            if (!(G & blocked) && __builtin_popcountll(S | G) <= kBQ) {
-                S |= G;
-                members.push_back(j);
-                done[j] = 1;
-            } else {
-                blocked |= G;
-                if ((blocked & all) == all) break;
-            }
+        size_t tried = 0;
+        for (size_t seed = first; seed < n && tried < kSeeds; ++seed) {
+            if (done[seed]) continue;
+            ++tried;
+            std::vector<size_t> m = block_trial(lg, done, first, seed, all);
+            if (m.size() > members.size()) members.swap(m);
+        }
+        uint64_t S = 0;
+        for (size_t j : members) {
+            S |= lg[j].sup;
+            done[j] = 1;
         }
         for (int q = 0; q < (int)L && __builtin_popcountll(S) < kBQ; ++q) S |= 1ull << q;  // pad to 5 qubits
         Block b;

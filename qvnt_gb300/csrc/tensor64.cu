@@ -226,6 +226,29 @@ __device__ __forceinline__ bool prep_tile(const double2* tiles, uint32_t b, uint
     return true;
 }
 
+// Read back level L of the thread's 2 NA output reals (once digit L's products are done, the last
+// to add to that level) into the 64-bit sums: acc += level x 2^(8 (5 - L)), from the magic-number
+// bits (their constants are removed at the end, modulo 2^64).
+template <int L, int NA>
+__device__ __forceinline__ void read_level(uint64_t (&acc)[2 * NA], uint32_t taddr) {
+#pragma unroll
+    for (int part = 0; part < NA / 4; ++part) {
+        uint32_t v[8];
+        tmem_ld8(taddr + 64u * (uint32_t)L + 8u * (uint32_t)part, v);
+        tmem_ld_wait();
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+            const int k = 8 * part + kk;
+            const float f = __uint_as_float(v[kk]);
+            if (L == 0) acc[k] = (uint64_t)mbits(f) << 32;
+            else if (L == 1) acc[k] = (uint64_t)((uint32_t)(acc[k] >> 32) * 256u + mbits(f)) << 32;
+            else if (L < 5) acc[k] += (uint64_t)mbits(f) << (8 * (5 - L));
+            else if (L == 5) acc[k] += 2ull * mbits_even(f);
+            else acc[k] += mbits_div256(f);
+        }
+    }
+}
+
 template <int kRegs, int NA>
 __global__ void __maxnreg__(kRegs)
     tensor64_pass_kernel(double2* __restrict__ psi, const unsigned char* __restrict__ wts,
@@ -405,52 +428,50 @@ __global__ void __maxnreg__(kRegs)
             put_digit<0, NA>(y, slot0, &bar_full[0], lane);
             put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
         }
+        const uint32_t acc_addr = tmem + lane_addr + 2u * NA * cg;  // this thread's columns of level 0
         for (uint32_t i = 0; ok && i < my_tiles; ++i) {
             const uint32_t b = i & 1u;
-            // a slot takes digit s once the MMAs of digit s - 2 are done
+            // a slot takes digit s once the MMAs of digit s - 2 are done; level l is final once digit
+            // l's are, and is read back then
+            uint64_t acc[2 * NA];
             ok = wait_mma(0);
-            if (ok) put_digit<2, NA>(y, slot0, &bar_full[0], lane);
-            if (ok) ok = wait_mma(1);
-            if (ok) put_digit<3, NA>(y, slot0 + 32u, &bar_full[1], lane);
-            if (ok) ok = wait_mma(0);
-            if (ok) put_digit<4, NA>(y, slot0, &bar_full[0], lane);
-            if (ok) ok = wait_mma(1);
-            if (ok) put_digit<5, NA>(y, slot0 + 32u, &bar_full[1], lane);
-            if (ok) ok = wait_mma(0);
-            if (ok) put_digit<6, NA>(y, slot0, &bar_full[0], lane);
+            if (ok) {
+                read_level<0, NA>(acc, acc_addr);
+                put_digit<2, NA>(y, slot0, &bar_full[0], lane);
+                ok = wait_mma(1);
+            }
+            if (ok) {
+                read_level<1, NA>(acc, acc_addr);
+                put_digit<3, NA>(y, slot0 + 32u, &bar_full[1], lane);
+                ok = wait_mma(0);
+            }
+            if (ok) {
+                read_level<2, NA>(acc, acc_addr);
+                put_digit<4, NA>(y, slot0, &bar_full[0], lane);
+                ok = wait_mma(1);
+            }
+            if (ok) {
+                read_level<3, NA>(acc, acc_addr);
+                put_digit<5, NA>(y, slot0 + 32u, &bar_full[1], lane);
+                ok = wait_mma(0);
+            }
+            if (ok) {
+                read_level<4, NA>(acc, acc_addr);
+                put_digit<6, NA>(y, slot0, &bar_full[0], lane);
+            }
             if (!ok) break;
             // the next tile's slices while this tile's last digits multiply
             const uint32_t E_this = E;
             const bool has_next = i + 1 < my_tiles;
             if (has_next)
                 ok = prep_tile<NA>(tiles, b ^ 1u, ph_tma, mrow, rp, s_exp, cg, quad, row, y, E, abort_flag, err, bar_tma,
-                               counter ? s_loads_seen : nullptr);
-            // every MMA of this tile done: the commits of digits 6 (slot 0) and 5 (slot 1)
-            const bool done0 = wait_mma(0);
-            const bool done1 = wait_mma(1);
-            if (!(done0 && done1)) break;
-            // the seven levels of this thread's 2 NA output reals: sum of level x 2^(8 (5 - l)), from the
-            // magic-number bits (their constants removed at the end, modulo 2^64)
-            uint64_t acc[2 * NA];
-#pragma unroll
-            for (int l = 0; l < kDigits; ++l) {
-#pragma unroll
-                for (int part = 0; part < NA / 4; ++part) {
-                    uint32_t v[8];
-                    tmem_ld8(tmem + lane_addr + 64u * (uint32_t)l + 2u * NA * cg + 8u * (uint32_t)part, v);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int kk = 0; kk < 8; ++kk) {
-                        const int k = 8 * part + kk;
-                        const float f = __uint_as_float(v[kk]);
-                        if (l == 0) acc[k] = (uint64_t)mbits(f) << 32;
-                        else if (l == 1) acc[k] = (uint64_t)((uint32_t)(acc[k] >> 32) * 256u + mbits(f)) << 32;
-                        else if (l < 5) acc[k] += (uint64_t)mbits(f) << (8 * (5 - l));
-                        else if (l == 5) acc[k] += 2ull * mbits_even(f);
-                        else acc[k] += mbits_div256(f);
-                    }
-                }
-            }
+                                   counter ? s_loads_seen : nullptr);
+            // levels 5 and 6: the commits of digits 5 (slot 1) and 6 (slot 0), the last of this tile
+            const bool done5 = wait_mma(1);
+            if (done5) read_level<5, NA>(acc, acc_addr);
+            const bool done6 = wait_mma(0);
+            if (!(done5 && done6)) break;
+            read_level<6, NA>(acc, acc_addr);
             tc_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive(&bar_acc);

@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "golden", "config2_26q.npz")
 ABS_TOL = 1e-12
 REL_FUSED = 1e-12  # measured 2.05e-13 at 26 qubits (2,633 gates)
-REL_T64 = 2e-13  # measured 4.9e-14 at 26 qubits
+REL_T64 = 2e-13  # measured 1.16e-13 at 26 qubits (288-block plan)
 
 
 @pytest.fixture(scope="module")
