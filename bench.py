@@ -71,8 +71,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1, help="steps of the plain f64 GPU path (0 = skip)")
-    ap.add_argument("--forms", default="df64,batch,serve,precision",
-                    help="extra forms to measure: df64, batch, serve, precision (empty = none)")
+    ap.add_argument("--forms", default="plain,df64,batch,serve,precision",
+                    help="extra forms to measure: plain, df64, batch, serve, precision (empty = none)")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
@@ -361,15 +361,59 @@ def bench_precision(ctx, n=32, depth=60, n_ref=30):
                               "sample": "first %d gates at %d qubits, extrapolated per gate" % (sample, n)}}
 
 
-def bench_serve(ctx, rate, seconds):
+def bench_plain_kernels(ctx, n=30, reps=8):
+    """The PLAIN engine's kernels gate by gate on a 30-qubit register: per case (kind, target
+    qubits, controls) the mean CUDA-event time of one launch and the HBM bandwidth of the bytes it
+    must move (read + write of the 2^(n - controls) amplitudes it touches; the SWAP family touches
+    only the half whose two bits differ).  Low targets (all below qubit 5) run the warp-shuffle
+    kernel, the others the strided-orbit kernel."""
+    from qvnt_gb300 import ENGINE_PLAIN, QReg, op
+    from qvnt_gb300.operator import MultiOp
+    cases = [("x", op.x(1 << 0), 0, 1.0), ("x", op.x(1 << 20), 0, 1.0), ("x", op.x(0b10110), 0, 1.0),
+             ("z", op.z(1 << 3), 0, 1.0), ("s", op.s(1 << 25), 0, 1.0), ("t", op.t(1 << 2), 0, 1.0),
+             ("rx", op.rx(0.3, 1 << 1), 0, 1.0), ("rx", op.rx(0.3, 1 << 22), 0, 1.0),
+             ("ry", op.ry(0.7, 1 << 4), 0, 1.0), ("rz", op.rz(0.7, 1 << 28), 0, 1.0),
+             ("h1", op.h(1 << 0), 0, 1.0), ("h1", op.h(1 << 29), 0, 1.0),
+             ("h2", op.h(0b11), 0, 1.0), ("h2", op.h((1 << 12) | (1 << 27)), 0, 1.0),
+             ("rxx", op.rxx(1.1, 0b1010), 0, 1.0), ("rxx", op.rxx(1.1, (1 << 8) | (1 << 21)), 0, 1.0),
+             ("rzz", op.rzz(1.1, (1 << 5) | (1 << 20)), 0, 1.0),
+             ("swap", op.swap(0b11), 0, 0.5), ("swap", op.swap((1 << 10) | (1 << 25)), 0, 0.5),
+             ("toffoli", op.x(1 << 7).c((1 << 3) | (1 << 19)), 2, 1.0)]
+    q = QReg(n, 0, ctx=ctx)
+    q.set_engine(ENGINE_PLAIN)
+    q.apply(op.h((1 << n) - 1))
+    out = []
+    for name, one, ctrls, frac in cases:
+        ops = MultiOp(list(one.ops) * reps)
+        q.apply(ops)  # warm-up
+        q.sync()
+        q.kernel_timing(enable=1)
+        q.apply(ops)
+        ms, k = q.kernel_timing(enable=0)
+        per = ms / k
+        moved = 2 * (1 << (n - ctrls)) * AMP_BYTES * frac
+        tg = one.ops[0].g
+        out.append({"gate": name, "targets": hex(tg.a_mask | tg.b_mask), "ctrl": hex(tg.ctrl),
+                    "kernel": "diagonal" if name in ("z", "s", "t", "rz", "rzz") else
+                    "shuffle" if ((tg.a_mask | tg.b_mask) < 32 and not (tg.ctrl & 31) and name != "swap") else "orbit",
+                    "ms": per, "gbs": moved / (per / 1e3) / 1e9})
+    q.close()
+    return {"workload": "one gate of each case on a %d-qubit PLAIN register, %d launches each" % (n, reps),
+            "cases": out}
+
+
+def bench_serve(ctx, rate, seconds, engine=None):
     """Serving form: Poisson arrivals at `rate`/s for `seconds` s (n log-uniform [10, 28], depth
     uniform [5, 100] over 1-3 apply/measure rounds, 150 GB HBM budget, 32 slots, queue of 1024);
-    then 5 s to drain.  Latency = completion - scheduled arrival."""
+    then 5 s to drain.  Latency = completion - scheduled arrival.  The server's registers run on
+    `engine` (the context's default engine when None)."""
     import numpy as np
     from qvnt_gb300.circuits import serve_requests
     from qvnt_gb300.serve import Server
 
     max_queue = 1024
+    if engine is not None:
+        ctx.set_engine(engine)
     s = Server(budget_bytes=150 * 10**9, slots=32, max_queue=max_queue, ctx=ctx)
     t0 = s.clock()
     offered = shed = 0
@@ -601,6 +645,7 @@ def main():
                "d2h_bytes_per_step": length * AMP_BYTES, "engine": args.engine}
 
     forms = {}
+    ctx.set_engine(ENGINE_FUSED)  # the forms choose their engines themselves
     if args.no_e2e:  # the e2e leg has already released the 30-qubit register
         q.close()
         del q
@@ -608,16 +653,29 @@ def main():
         torch.cuda.synchronize()
         for form in [f for f in args.forms.split(",") if f]:
             try:
-                if form == "df64":
+                if form == "plain":
+                    forms["plain_kernels"] = bench_plain_kernels(ctx, n)
+                elif form == "df64":
                     if engine != ENGINE_FUSED:
                         forms["df64"] = bench_df64(ctx, garr, ngates, n, max(1, min(args.steps, 3)))
                 elif form == "batch":
                     forms["batch"] = bench_batch(ctx, args.batch_count, max(1, min(args.steps, 5)), args.batch_fusion)
                 elif form == "serve":
-                    forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds)
+                    # the double-float engine with one CTA per tile, so that small requests' tiles
+                    # interleave with large requests' passes
+                    forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds, ENGINE_FUSED)
+                    forms["serve"]["engine"] = "fused (double-float)"
                     # the same request mix at a rate one GPU sustains (the configured rate is about
                     # two orders of magnitude above its capacity for this mix)
-                    forms["serve"]["at_sustainable_rate"] = bench_serve(ctx, 4.0, min(args.serve_seconds, 20.0))
+                    forms["serve"]["at_sustainable_rate"] = bench_serve(ctx, 4.0, min(args.serve_seconds, 20.0),
+                                                                        ENGINE_FUSED)
+                    # the plain f64 GPU path serving the same mix (20 s of the same Poisson stream)
+                    pl = bench_serve(ctx, args.serve_rate, min(args.serve_seconds, 20.0), ENGINE_PLAIN)
+                    forms["serve"]["plain_f64_gpu"] = {
+                        "served_circuits_per_s": pl["served_circuits_per_s"], "p50_ms": pl["p50_ms"],
+                        "p99_ms": pl["p99_ms"], "completed": pl["completed"],
+                        "sample": "the same Poisson mix for %.0f s on the PLAIN engine" % min(args.serve_seconds, 20.0)}
+                    ctx.set_engine(ENGINE_FUSED)
                 elif form == "precision":
                     forms["precision"] = bench_precision(ctx, args.precision_qubits, args.precision_depth,
                                                          args.precision_ref_qubits)

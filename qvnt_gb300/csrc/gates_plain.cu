@@ -7,8 +7,11 @@
 // enumerated by bit insertion: the target bits are inserted as 0 and the control bits as 1 into a
 // dense counter, so a gate with c controls touches only 2^(n-c) amplitudes.  Built with
 // --fmad=false: on IEEE f64 storage the results are bit-identical to qvnt's non-fast-math
-// arithmetic.  The same kernels serve double-float registers for gates the fused engine does not
-// tile (AccDF64 converts on load and store).
+// arithmetic.  Gates whose targets all lie in the five lowest qubits (and whose controls do not)
+// run with one amplitude per thread and the orbit partners taken from other lanes by warp shuffles
+// (plain_shfl_kernel); the others read an orbit's members from the two (or four) strided halves of
+// the state, each a coalesced 16-byte load per thread.  The same kernels serve double-float
+// registers for gates the fused engine does not tile (AccDF64 converts on load and store).
 #include <algorithm>
 #include <vector>
 
@@ -20,17 +23,21 @@ namespace qvnt {
 
 namespace {
 
-constexpr int kUnroll = 2;
+// Orbits in flight per thread: four one-amplitude orbits (diagonal gates), two of the others.
+template <int SHAPE>
+constexpr int unroll_of() { return SHAPE == 1 ? 4 : 2; }
+constexpr int kUnroll = 2;  // grid sizing
 
 template <int SHAPE, class Acc>
 __global__ void __launch_bounds__(256) plain_gate_kernel(double2* __restrict__ psi, const DevGate g, const Enum e,
                                                          const uint64_t pmask) {
+    constexpr int kU = unroll_of<SHAPE>();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t j0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j0 < e.count; j0 += stride * kUnroll) {
-        amp_t v[kUnroll][SHAPE];
-        uint64_t base[kUnroll];
+    for (uint64_t j0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j0 < e.count; j0 += stride * kU) {
+        amp_t v[kU][SHAPE];
+        uint64_t base[kU];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
+        for (int u = 0; u < kU; ++u) {
             const uint64_t j = j0 + u * stride;
             if (j < e.count) {
                 base[u] = enum_index(e, j);
@@ -48,7 +55,7 @@ __global__ void __launch_bounds__(256) plain_gate_kernel(double2* __restrict__ p
             }
         }
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
+        for (int u = 0; u < kU; ++u) {
             const uint64_t j = j0 + u * stride;
             if (j >= e.count) continue;
             const uint64_t i0 = base[u];
@@ -79,6 +86,54 @@ __global__ void __launch_bounds__(256) plain_gate_kernel(double2* __restrict__ p
                 Acc::store(psi, i0 | b, o2);
                 Acc::store(psi, i0 | a | b, o3);
             }
+        }
+    }
+}
+
+// Orbits inside a warp: when every target bit of the gate is below 5 and no control bit is, lane l
+// holds amplitude (warp base + l) and the orbit partners of an amplitude sit in lanes l ^ m.  Each
+// thread loads its one amplitude (a warp reads 512 contiguous bytes), takes the partners' values
+// from their lanes (__shfl_xor_sync), evaluates qvnt's atomic_op for its own index and stores it.
+// NP = 1: pairs (i, i ^ m1); NP = 3: quads (i, i ^ m1, i ^ m2, i ^ m1 ^ m2).  e.count is a multiple
+// of 32, so a warp is either wholly inside the enumeration or wholly past it.
+__device__ __forceinline__ double2 shfl_xor_amp(double2 v, uint32_t m) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, (int)m), __shfl_xor_sync(0xffffffffu, v.y, (int)m));
+}
+
+template <int NP, class Acc>
+__global__ void __launch_bounds__(256) plain_shfl_kernel(double2* __restrict__ psi, const DevGate g, const Enum e,
+                                                         const uint32_t m1, const uint32_t m2) {
+    constexpr int U = 4;  // amplitudes in flight per thread
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j0 < e.count; j0 += stride * U) {
+        uint64_t idx[U];
+        amp_t x[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint64_t j = j0 + u * stride;
+            if (j < e.count) {  // the same for every lane of the warp
+                idx[u] = enum_index(e, j);
+                x[u] = Acc::load(psi, idx[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (j0 + u * stride >= e.count) break;
+            const uint64_t i = idx[u];
+            const amp_t xi = x[u];
+            const amp_t y1 = shfl_xor_amp(xi, m1);
+            amp_t out;
+            if (NP == 1) {
+                out = atomic_op(g, i, [&](uint64_t k) { return k == i ? xi : y1; });
+            } else {
+                const amp_t y2 = shfl_xor_amp(xi, m2);
+                const amp_t y3 = shfl_xor_amp(xi, m1 ^ m2);
+                out = atomic_op(g, i, [&](uint64_t k) {
+                    const uint64_t d = k ^ i;
+                    return d == 0 ? xi : (d == m1 ? y1 : (d == m2 ? y2 : y3));
+                });
+            }
+            Acc::store(psi, i, out);
         }
     }
 }
@@ -120,6 +175,21 @@ unsigned grid_for(uint64_t work, const Geometry& geo, int threads) {
     return (unsigned)want;
 }
 
+template <int NP>
+void launch_shfl(int fmt, unsigned grid, cudaStream_t stream, double2* psi, const DevGate& g, const Enum& e, uint32_t m1,
+                 uint32_t m2) {
+    if (fmt == FMT_DF64)
+        plain_shfl_kernel<NP, AccDF64><<<grid, 256, 0, stream>>>(psi, g, e, m1, m2);
+    else
+        plain_shfl_kernel<NP, AccF64><<<grid, 256, 0, stream>>>(psi, g, e, m1, m2);
+}
+
+// The in-warp form applies when the orbit's masks stay inside a lane's five low index bits, the
+// controls do not (lane = index bits 0..4), and the enumeration covers whole warps.
+bool shfl_fits(uint64_t targets, uint64_t ctrl, uint64_t count) {
+    return targets != 0 && targets < 32 && (ctrl & 31ull) == 0 && count >= 32 && (count & 31ull) == 0;
+}
+
 template <int SHAPE>
 void launch_shape(int fmt, unsigned grid, cudaStream_t stream, double2* psi, const DevGate& g, const Enum& e,
                   uint64_t pmask) {
@@ -156,6 +226,11 @@ int launch_plain_gate(double2* psi, int fmt, uint64_t len, const DevGate& g, cud
     }
     case QVNT_GATE_X: case QVNT_GATE_Y: case QVNT_GATE_RX: case QVNT_GATE_RY: case QVNT_GATE_H1:
     case QVNT_GATE_U1: case QVNT_GATE_RXX: case QVNT_GATE_RYY: {
+        const Enum all = make_enum(len, ctrl, ctrl);
+        if (shfl_fits(g.a, ctrl, all.count)) {  // pairs (i, i ^ a) inside a warp
+            launch_shfl<1>(fmt, grid_for(all.count, geo, threads), stream, psi, g, all, (uint32_t)g.a, 0);
+            break;
+        }
         const uint64_t pivot = 1ull << high_bit(g.a);
         Enum e = make_enum(len, ctrl | pivot, ctrl);
         launch_shape<2>(fmt, grid_for(e.count, geo, threads), stream, psi, g, e, g.a);
@@ -169,6 +244,11 @@ int launch_plain_gate(double2* psi, int fmt, uint64_t len, const DevGate& g, cud
         break;
     }
     case QVNT_GATE_H2: case QVNT_GATE_U2: {
+        const Enum all = make_enum(len, ctrl, ctrl);
+        if (shfl_fits(g.a | g.b, ctrl, all.count)) {  // quads (i, i ^ a, i ^ b, i ^ a ^ b) inside a warp
+            launch_shfl<3>(fmt, grid_for(all.count, geo, threads), stream, psi, g, all, (uint32_t)g.a, (uint32_t)g.b);
+            break;
+        }
         Enum e = make_enum(len, ctrl | g.a | g.b, ctrl);
         launch_shape<4>(fmt, grid_for(e.count, geo, threads), stream, psi, g, e, 0);
         break;

@@ -231,21 +231,23 @@ __device__ __forceinline__ bool prep_tile(const double2* tiles, uint32_t b, uint
 // bits (their constants are removed at the end, modulo 2^64).
 template <int L, int NA>
 __device__ __forceinline__ void read_level(uint64_t (&acc)[2 * NA], uint32_t taddr) {
+    uint32_t v[2 * NA];  // the level's 2 NA columns of this lane, loaded together
 #pragma unroll
     for (int part = 0; part < NA / 4; ++part) {
-        uint32_t v[8];
-        tmem_ld8(taddr + 64u * (uint32_t)L + 8u * (uint32_t)part, v);
-        tmem_ld_wait();
+        uint32_t w[8];
+        tmem_ld8(taddr + 64u * (uint32_t)L + 8u * (uint32_t)part, w);
 #pragma unroll
-        for (int kk = 0; kk < 8; ++kk) {
-            const int k = 8 * part + kk;
-            const float f = __uint_as_float(v[kk]);
-            if (L == 0) acc[k] = (uint64_t)mbits(f) << 32;
-            else if (L == 1) acc[k] = (uint64_t)((uint32_t)(acc[k] >> 32) * 256u + mbits(f)) << 32;
-            else if (L < 5) acc[k] += (uint64_t)mbits(f) << (8 * (5 - L));
-            else if (L == 5) acc[k] += 2ull * mbits_even(f);
-            else acc[k] += mbits_div256(f);
-        }
+        for (int kk = 0; kk < 8; ++kk) v[8 * part + kk] = w[kk];
+    }
+    tmem_ld_wait();
+#pragma unroll
+    for (int k = 0; k < 2 * NA; ++k) {
+        const float f = __uint_as_float(v[k]);
+        if (L == 0) acc[k] = (uint64_t)mbits(f) << 32;
+        else if (L == 1) acc[k] = (uint64_t)((uint32_t)(acc[k] >> 32) * 256u + mbits(f)) << 32;
+        else if (L < 5) acc[k] += (uint64_t)mbits(f) << (8 * (5 - L));
+        else if (L == 5) acc[k] += 2ull * mbits_even(f);
+        else acc[k] += mbits_div256(f);
     }
 }
 
