@@ -20,7 +20,13 @@ struct EngineBuffers {
     size_t d_bytes = 0;
     void* h_buf = nullptr;  // pinned host mirror for the upload
     size_t h_bytes = 0;
+    cudaEvent_t uploaded = nullptr;  // recorded on the register's stream after the last upload from h_buf
     void release();
+    // Buffers of at least `bytes`; h_buf may be written once this returns (the last upload from it is
+    // done: the host waits for that upload only, not for the stream's other work).
+    int acquire(size_t bytes, cudaStream_t stream);
+    // Queues the upload of `bytes` from h_buf to d_buf on `stream` and records `uploaded`.
+    int upload(size_t bytes, cudaStream_t stream);
 };
 
 }  // namespace qvnt

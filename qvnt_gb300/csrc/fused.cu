@@ -1722,9 +1722,31 @@ __global__ void batch_basis_kernel(float4* __restrict__ psi, const uint64_t* __r
 void EngineBuffers::release() {
     if (d_buf) cudaFree(d_buf);
     if (h_buf) cudaFreeHost(h_buf);
+    if (uploaded) cudaEventDestroy(uploaded);
     d_buf = nullptr;
     h_buf = nullptr;
+    uploaded = nullptr;
     d_bytes = h_bytes = 0;
+}
+
+int EngineBuffers::acquire(size_t bytes, cudaStream_t stream) {
+    if (d_bytes >= bytes && h_bytes >= bytes) {
+        if (uploaded) QVNT_CUDA_TRY(cudaEventSynchronize(uploaded));
+        return QVNT_OK;
+    }
+    if (d_buf || h_buf) QVNT_CUDA_TRY(cudaStreamSynchronize(stream));  // passes may still read d_buf
+    release();
+    QVNT_CUDA_TRY(cudaMalloc(&d_buf, bytes));
+    QVNT_CUDA_TRY(cudaMallocHost(&h_buf, bytes));
+    d_bytes = h_bytes = bytes;
+    return QVNT_OK;
+}
+
+int EngineBuffers::upload(size_t bytes, cudaStream_t stream) {
+    QVNT_CUDA_TRY(cudaMemcpyAsync(d_buf, h_buf, bytes, cudaMemcpyHostToDevice, stream));
+    if (!uploaded) QVNT_CUDA_TRY(cudaEventCreateWithFlags(&uploaded, cudaEventDisableTiming));
+    QVNT_CUDA_TRY(cudaEventRecord(uploaded, stream));
+    return QVNT_OK;
 }
 
 int apply_fused(qvnt_reg* r, const qvnt_gate* gates, size_t count) {

@@ -381,16 +381,10 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     // weights of every block, uploaded once per apply call
     const size_t wfl = blocks.size() * 2 * kWFloats;
     EngineBuffers& fs = r->bufs;
-    if (fs.h_buf) QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));  // the last upload has left h_buf
-    if (fs.d_bytes < wfl * 4) {
-        fs.release();
-        QVNT_CUDA_TRY(cudaMalloc(&fs.d_buf, wfl * 4));
-        QVNT_CUDA_TRY(cudaMallocHost(&fs.h_buf, wfl * 4));
-        fs.d_bytes = fs.h_bytes = wfl * 4;
-    }
+    TRY_LAUNCH(fs.acquire(wfl * 4, r->stream));
     float* hw = static_cast<float*>(fs.h_buf);
     for (size_t i = 0; i < blocks.size(); ++i) block_weights(blocks[i], hw + i * 2 * kWFloats, hw + i * 2 * kWFloats + kWFloats);
-    QVNT_CUDA_TRY(cudaMemcpyAsync(fs.d_buf, fs.h_buf, wfl * 4, cudaMemcpyHostToDevice, r->stream));
+    TRY_LAUNCH(fs.upload(wfl * 4, r->stream));
     // the norm to keep (FP64)
     double* d_norm0 = reinterpret_cast<double*>(r->d_small) + 5;
     double* d_norm = reinterpret_cast<double*>(r->d_small) + 6;

@@ -519,11 +519,20 @@ uint16_t fp16_of_small_int(int d) {  // exact for |d| <= 2048
     return (uint16_t)(sgn | ((uint32_t)(e + 15) << 10) | mant);
 }
 
+// fp16 bits of the digit byte c - 128, for every byte c.
+struct DigitTable {
+    uint16_t h[256];
+    DigitTable() {
+        for (int c = 0; c < 256; ++c) h[c] = fp16_of_small_int(c - 128);
+    }
+};
+
 // A block's weights: the real 64 x 64 form W[2r' + c'][2r + c] = ((Re, -Im), (Im, Re)) of U[r'][r]
 // (row = output real, column = input real); per row its largest exponent F, the 53-bit integers
 // round(W * 2^(1075 - F)) and their seven balanced base-256 digits as fp16 in the operand layout
 // (digit t = 0 most significant), then the 64 row exponents.
 void block_weights64(const dense::Block& b, unsigned char* out) {
+    static const DigitTable digits;
     static thread_local double W[64][64];
     for (uint32_t rp = 0; rp < 32; ++rp)
         for (uint32_t r = 0; r < 32; ++r) {
@@ -549,10 +558,8 @@ void block_weights64(const dense::Block& b, unsigned char* out) {
             memcpy(&bits, &W[n][k], 8);
             if (fmax > 0 && ((bits >> 52) & 0x7ff) != 0) X = std::llrint(std::ldexp(W[n][k], 1075 - fmax));
             const uint64_t Y = (uint64_t)X + kBias;
-            for (int t = 0; t < kDigits; ++t) {
-                const int d = (int)((Y >> (8 * (6 - t))) & 0xffu) - 128;
-                dig[(size_t)t * (kWDigitBytes / 2) + w_off16(n, k)] = fp16_of_small_int(d);
-            }
+            for (int t = 0; t < kDigits; ++t)
+                dig[(size_t)t * (kWDigitBytes / 2) + w_off16(n, k)] = digits.h[(Y >> (8 * (6 - t))) & 0xffu];
         }
     }
 }
@@ -633,16 +640,10 @@ int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     if (passes.empty()) return QVNT_OK;
     const size_t wbytes = blocks.size() * (size_t)kWBlockBytes;
     EngineBuffers& fs = r->bufs;
-    if (fs.h_buf) QVNT_CUDA_TRY(cudaStreamSynchronize(r->stream));  // the last upload has left h_buf
-    if (fs.d_bytes < wbytes || fs.h_bytes < wbytes) {
-        fs.release();
-        QVNT_CUDA_TRY(cudaMalloc(&fs.d_buf, wbytes));
-        QVNT_CUDA_TRY(cudaMallocHost(&fs.h_buf, wbytes));
-        fs.d_bytes = fs.h_bytes = wbytes;
-    }
+    TRY_T(fs.acquire(wbytes, r->stream));
     unsigned char* hw = static_cast<unsigned char*>(fs.h_buf);
     for (size_t i = 0; i < blocks.size(); ++i) block_weights64(blocks[i], hw + i * (size_t)kWBlockBytes);
-    QVNT_CUDA_TRY(cudaMemcpyAsync(fs.d_buf, fs.h_buf, wbytes, cudaMemcpyHostToDevice, r->stream));
+    TRY_T(fs.upload(wbytes, r->stream));
     static const PassKernel kern = pick_kernel();
     if (!kern.fn) return set_error(QVNT_ERR_CUDA, "tensor64 kernel: %s", kern.why);
     int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
