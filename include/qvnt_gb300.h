@@ -99,8 +99,9 @@ typedef struct qvnt_gate {
 typedef struct qvnt_ctx qvnt_ctx;
 typedef struct qvnt_reg qvnt_reg;
 
-/* Engines a register can run its gate queue on.
- *   FUSED  (default) groups runs of gates into fused passes staged through shared memory.
+/* Engines a register can run its gate queue on (a context's default: TENSOR64).
+ *   FUSED  groups runs of gates into fused passes staged through shared memory, in double-float
+ *          (pairs of FP32, 48-bit significand).
  *   PLAIN  runs one in-place FP64 pass per `SingleOp`, in qvnt's own operand order; its amplitudes
  *          are bit-identical to qvnt's non-fast-math arithmetic.  It is the plain f64 GPU path.
  *   PRECISION keeps complex<f32> amplitudes (8 B) and fuses runs of gates into dense 5-qubit blocks
@@ -131,7 +132,7 @@ int qvnt_ctx_destroy(qvnt_ctx* ctx);
 /* Free device memory and the total in bytes, as the CUDA runtime reports them for this device. */
 int qvnt_ctx_mem_info(qvnt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
 /* Engine (enum qvnt_engine) of the registers qvnt_reg_create makes on this context and of the
- * scratch register of qvnt_apply_host (which runs PRECISION requests on FUSED); default FUSED.
+ * scratch register of qvnt_apply_host (which runs PRECISION requests on FUSED); default TENSOR64.
  * No counterpart in the reference (its one CPU path has no choice to make). */
 int qvnt_ctx_set_engine(qvnt_ctx* ctx, int engine);
 

@@ -36,7 +36,7 @@ struct qvnt_ctx {
     int device = 0;
     qvnt::Geometry geo;
     int smem_optin = 0;
-    int default_engine = QVNT_ENGINE_FUSED;
+    int default_engine = QVNT_ENGINE_TENSOR64;  // f64 semantics by default
     std::mutex host_mu;
     struct qvnt_reg* host_reg = nullptr;  // scratch register of qvnt_apply_host
 };

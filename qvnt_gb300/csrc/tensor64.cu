@@ -668,7 +668,8 @@ int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
         for (uint32_t q = 0; q < L; ++q)
             if ((blk.sup >> q) & 1ull) P.bits[jj++] = (uint8_t)pos_of[q];
         P.w_off = bi * (uint64_t)kWBlockBytes;
-        const uint64_t grid = std::min<uint64_t>((uint64_t)r->ctx->geo.sms, P.ntiles);
+        // persistent (one CTA per SM), or one CTA per tile for registers that share the GPU
+        const uint64_t grid = r->tile_grid ? P.ntiles : std::min<uint64_t>((uint64_t)r->ctx->geo.sms, P.ntiles);
         cudaEvent_t stop = nullptr;
         TRY_T(timing_begin(r, &stop));
         kern.fn<<<(unsigned)grid, kern.threads, kSmemDyn, r->stream>>>(r->psi, static_cast<const unsigned char*>(fs.d_buf), P,

@@ -28,8 +28,8 @@ impl GpuContext {
         Ok(Arc::new(GpuContext { h }))
     }
 
-    /// Engine of the registers this context makes and of `apply_host` (default: FUSED; the f64
-    /// tensor-core engine is `ffi::ENGINE_TENSOR64`, the one-pass-per-gate IEEE path `ENGINE_PLAIN`).
+    /// Engine of the registers this context makes and of `apply_host` (default: the f64 tensor-core
+    /// engine `ffi::ENGINE_TENSOR64`; the one-pass-per-gate IEEE path is `ENGINE_PLAIN`).
     pub fn set_engine(&self, engine: i32) -> Result<(), GpuError> {
         check(unsafe { ffi::qvnt_ctx_set_engine(self.h, engine) })
     }
