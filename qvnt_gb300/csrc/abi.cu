@@ -117,8 +117,8 @@ int reg_alloc(qvnt_reg* r) {
         r->scratch = nullptr;
         return set_cuda_error(e, "cudaMalloc(scratch)");
     }
-    QVNT_CUDA_TRY(cudaMalloc(&r->d_small, 64));
-    QVNT_CUDA_TRY(cudaMemsetAsync(r->d_small, 0, 64, r->stream));
+    QVNT_CUDA_TRY(cudaMalloc(&r->d_small, 128));
+    QVNT_CUDA_TRY(cudaMemsetAsync(r->d_small, 0, 128, r->stream));
     QVNT_CUDA_TRY(cudaMallocHost(&r->h_small, 64));
     return QVNT_OK;
 }

@@ -51,7 +51,7 @@ struct qvnt_reg {
     double* scratch = nullptr;   // reduction partials
     void* staging = nullptr;     // device staging for host reads
     uint64_t staging_bytes = 0;
-    void* d_small = nullptr;     // 64 B of device results (index, status, sums)
+    void* d_small = nullptr;     // 128 B: device results (index, status, sums), then the tensor engine's scale ring
     void* h_small = nullptr;     // pinned 64 B host mirror
     cudaStream_t stream = nullptr;
     int engine = QVNT_ENGINE_FUSED;

@@ -1,37 +1,43 @@
 // Tensor-core f64 engine: IEEE f64 amplitudes in HBM (qvnt's Complex<f64> layout, the PLAIN
-// format), runs of gates fused into dense 5-qubit blocks (32 x 32 complex unitaries, the planner of
-// dense_blocks.h) and contracted on the tcgen05 tensor cores with 53-bit operands by exact integer
-// slicing (the Ozaki splitting of a matrix product into exactly representable digit products).
+// format) at every call boundary, runs of gates fused into dense 5-qubit blocks (32 x 32 complex
+// unitaries, the planner of dense_blocks.h) and contracted on the tcgen05 tensor cores with 54-bit
+// operands by exact integer slicing (the Ozaki splitting of a matrix product into exactly
+// representable digit products).
 //
-// Arithmetic.  Every operand row is scaled by a power of two to its largest element and rounded
-// to a 53-bit integer (an f64 significand): the state row X (the 32 amplitudes of one block
-// index group, 64 reals, scaled by the row's largest f64 exponent E) and the block matrix row W
-// (64 reals of one output component, scaled by its exponent F).  Each integer is split into seven
-// balanced base-256 digits in [-128, 127] (the top one in [-33, 32]), exact in fp16.  The block
-// product is the sum over digit pairs (s, t) of A_s * B_t^T weighted by 256^(12 - s - t); the 28
-// pairs with s + t <= 6 are issued as tcgen05.mma kind::f16 (M = 128 rows, N = 64, K = 16) into
-// seven FP32 accumulators in tensor memory, one per level l = s + t.  Every partial sum is an
-// integer below 2^23 in magnitude (at most l + 1 products of 64 terms of |digit| <= 128), so the
-// FP32 accumulation is exact.  Levels >= 7 are dropped (below 2^-55 of the row bound).  The
-// accumulators are read back (tcgen05.ld), turned into integers with a magic-number add, combined
-// into one 64-bit integer and rounded to the nearest f64 with the exponent E + F - 2094: per block
-// the result carries one rounding of the inputs (2^-53 of the row's power-of-two bound) and one
-// rounding to f64, no FP64 instruction is issued.
+// Number format between the passes of one apply call: 64-bit block floating point.  Every real
+// component is an int64 X with one scale 2^-S for the whole register (x = X 2^-S); before a pass
+// reads it, the register is renormalised (a uniform shift) so that its largest |X| is 2^53 .. 2^54.
+// A pass therefore rounds every component to 2^-54 .. 2^-55 of the register's largest component,
+// finer than IEEE f64 rounds the largest amplitudes.  The first pass of a call reads IEEE f64 (sliced
+// against the register's largest exponent, found by a reduction kernel first) and the last one
+// writes IEEE f64, so only the passes in between see the integer format.
+//
+// Arithmetic of a pass.  The block matrix in its real 64 x 64 form W (row = output component,
+// column = input component) is held as round(W 2^55), |.| <= 2^55; it and the state are split into
+// seven balanced base-256 digits (|digit| <= 128), exact in fp16.  The product is the sum over digit
+// pairs (s, t) of A_s B_t^T weighted by 2^(96 - 8 (s + t)); the 34 pairs with s + t <= 7 are issued as
+// tcgen05.mma kind::f16 (M = 128 rows, N = 64, K = 16) into eight FP32 accumulators in tensor memory,
+// one per level l = s + t.  Every partial sum is an integer below 2^23 in magnitude (at most 7 products
+// of 64 terms of |digit product| <= 2^14, those with a top digit smaller), so the FP32 accumulation is
+// exact.  Levels >= 8 are dropped (2^-23 of an output unit per level-8 unit: typically 0.01 unit).
+// The accumulators are read back (tcgen05.ld), turned into integers (a magic-number add below 2^22,
+// an exact float-to-int conversion above), and combined into the output X' = sum_l L_l 2^(41 - 8 l)
+// with one rounding (of the levels 6 and 7 part); no FP64 instruction is issued.
 //
 // Kernel (one pass = one block): persistent CTAs, one per SM (tensor memory: all 512 columns), of
-// 18 warps (10 in the 16-amplitude layout) in three roles synchronised by mbarriers only.  Per tile of 4096 amplitudes (12 tile
-// qubits: the 7 lowest, so a tile is 2 KB runs, plus the block's):
+// 18 warps (10 in the 16-amplitude layout) in three roles synchronised by mbarriers only.  Per tile of
+// 4096 amplitudes (12 tile qubits: the 7 lowest, so a tile is 2 KB runs, plus the block's):
 //   * the copy warp keeps two shared-memory tile buffers filled with TMA bulk loads and stores each
 //     tile once its results are written;
 //   * 16 math warps each take one operand row (lane quadrant) and 8 of its 32 amplitudes (or 8 warps
-//     and 16 amplitudes): the row exponent (with the row's other warps), the slices, and the digits stored one by one to
-//     two ping-pong operand slots in tensor memory (a slot takes digit s once the MMAs of digit s - 2
-//     are done); then the read-back of the seven levels and the rounding to f64;
+//     and 16 amplitudes): the digits, stored one by one to two ping-pong operand slots in tensor
+//     memory (a slot takes digit s once the MMAs of digit s - 2 are done); then the read-back of the
+//     eight levels and the output;
 //   * the MMA warp issues each digit's products once its slot is full and commits them to the
 //     slot's mbarrier.
-// The next tile is sliced while this tile's last digits multiply, and this tile's results are
-// rounded while the next tile's first digits multiply: the tensor pipe waits only for the read-back
-// of the accumulators.
+// Level l is final once digit l's products are done; level 7 accumulates in level 0's columns, which
+// the math warps release right after reading level 0.  The next tile is sliced while this tile's last
+// digits multiply, and this tile's results are written while the next tile's first digits multiply.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -71,12 +77,15 @@ struct Layout {
     static constexpr uint32_t kTmaWarp = kMathWarps + 1; // issues the tile copies
     static constexpr uint32_t kNT = 32 * (kMathWarps + 2);
 };
-constexpr int kDigits = 7;                      // base-256 digits per 53-bit operand
+constexpr int kDigits = 7;                      // base-256 digits per operand
+constexpr int kWScale = 55;                     // block matrices are held as round(W 2^55)
+constexpr int kTopBits = 54;                    // fixed-point inputs are renormalised to |X| <= 2^54
 constexpr uint32_t kWDigitBytes = 64 * 64 * 2;  // one fp16 digit matrix of a block (8 KB)
-constexpr uint32_t kWBlockBytes = kDigits * kWDigitBytes + 64 * 4;  // digits + 64 row exponents
+constexpr uint32_t kWBlockBytes = kDigits * kWDigitBytes;
 constexpr uint32_t kWaitLimit = 1u << 22;       // mbarrier polls before a wait gives up
 constexpr uint32_t kSlotCol = 448;              // tensor-memory columns: levels 0..6 at 64 l, slots 448 / 480
 constexpr uint64_t kBias = 0x80808080808080ull; // 128 in each of the 7 digit bytes
+constexpr uint32_t kMagic = 0x4B400000u;        // bits of 1.5 * 2^23
 constexpr size_t kSmemDyn = 2 * (size_t)kTileAmps * 16 + kWBlockBytes;
 
 // Instruction descriptor of kind::f16: FP32 accumulator, A and B fp16 and K-major, N = 64, M = 128.
@@ -89,9 +98,21 @@ __host__ __device__ constexpr uint32_t w_off16(uint32_t row, uint32_t k) {
     return (row >> 3) * 512u + (k >> 3) * 64u + (row & 7u) * 8u + (k & 7u);
 }
 
+// Register scale of one pass, in a ring of three per register (pass p reads slot p mod 3, writes the
+// next slot, and clears the one after it for pass p + 1).  mag: before the first pass of a call, the
+// largest biased f64 exponent of the state; after a fixed-point pass, the OR of its outputs' high
+// words in sign-magnitude-like form (x ^ (x >> 31)), whose bit length is that of the largest output.
+// S: the scale exponent (x = X 2^-S) of the outputs of the pass that wrote the slot.
+struct ScaleSlot {
+    uint32_t mag;
+    int32_t S;
+};
+
 struct TPassParams {
     uint64_t ntiles;
     uint64_t w_off;      // byte offset of the block's weights in the weight buffer
+    ScaleSlot* slots;    // the register's scale ring
+    uint32_t cur;        // slot this pass reads
     uint32_t c;          // tile qubits 0 .. c-1 are the register's lowest: runs of 2^c amplitudes
     uint32_t tq[kTQ];    // tile qubits, ascending
     uint8_t bits[dense::kBQ];  // tile-local bit of block bit j
@@ -106,9 +127,9 @@ __device__ __forceinline__ void mma_f16_ta(uint32_t d_tmem, uint32_t a_tmem, uin
         : "memory");
 }
 
-// 53-bit fixed point of x against the row exponent E (biased, >= x's): X = round(x * 2^(1075 - E)),
-// |X| < 2^53; returns Y = X + kBias, whose byte j minus 128 is the balanced digit j of X.  Zeros and
-// f64 subnormals give X = 0.
+// Fixed point of an IEEE f64 x against the register's largest exponent E (biased, >= x's):
+// X = round(x 2^(1075 - E)), |X| < 2^53; returns Y = X + kBias, whose byte j minus 128 is the
+// balanced digit j of X.  Zeros and f64 subnormals give X = 0.
 __device__ __forceinline__ uint64_t slice(double x, uint32_t E) {
     const uint64_t b = (uint64_t)__double_as_longlong(x);
     const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
@@ -121,29 +142,28 @@ __device__ __forceinline__ uint64_t slice(double x, uint32_t E) {
     return ((b >> 63) ? (0ull - v) : v) + kBias;
 }
 
-// Digit byte `byte` of two reals as a packed fp16 pair: fp16(1408 + c) has the bits 0x6580 + c for
-// a byte c, and subtracting 1536 leaves c - 128 exactly.
+// A fixed-point component renormalised by 2^sigma (a left shift, or a right shift rounding half up)
+// and biased for the digit split.
+__device__ __forceinline__ uint64_t renorm(long long X, int sigma) {
+    if (sigma > 0) X = (long long)((unsigned long long)X << sigma);
+    else if (sigma < 0) X = (X + (1ll << (-sigma - 1))) >> (-sigma);
+    return (uint64_t)X + kBias;
+}
+
+// Digit byte `byte` of two reals as a packed fp16 pair: fp16(1024 + c) has the bits 0x6400 + c for
+// a byte c, and subtracting 1152 leaves c - 128 exactly.
 __device__ __forceinline__ uint32_t digit_pair(uint64_t y0, uint64_t y1, int byte) {
     const uint32_t w0 = byte < 4 ? (uint32_t)y0 : (uint32_t)(y0 >> 32);
     const uint32_t w1 = byte < 4 ? (uint32_t)y1 : (uint32_t)(y1 >> 32);
     const uint32_t j = (uint32_t)(byte & 3);
-    const uint32_t two = __byte_perm(w0, w1, j | ((4u + j) << 4));  // bytes (c0, c1, ., .)
-    uint32_t h = __byte_perm(two, 0u, 0x4140u) + 0x65806580u;        // (c0, 0, c1, 0) + bias
+    uint32_t h = (__byte_perm(w0, w1, j | (j << 4) | ((4u + j) << 8) | ((4u + j) << 12)) & 0x00ff00ffu) | 0x64006400u;
     __half2 v = *reinterpret_cast<__half2*>(&h);
-    v = __hsub2(v, __halves2half2(__ushort_as_half((unsigned short)0x6600), __ushort_as_half((unsigned short)0x6600)));
+    v = __hsub2(v, __halves2half2(__ushort_as_half((unsigned short)0x6480), __ushort_as_half((unsigned short)0x6480)));
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-// An integer-valued float as the bits of f + M, which hold the integer plus a constant: M = 1.5 * 2^23
-// (exact for |f| < 2^22, bits - 0x4B400000), M = 1.5 * 2^24 (|f| < 2^23 to the nearest even:
-// 2 (bits - 0x4BC00000)), and f / 256 + 1.5 * 2^23 (round(f / 256)).
+// An integer-valued float f, |f| < 2^22, as the bits of f + 1.5 * 2^23: the integer plus kMagic.
 __device__ __forceinline__ uint32_t mbits(float f) { return __float_as_uint(f + 12582912.0f); }
-__device__ __forceinline__ uint32_t mbits_even(float f) { return __float_as_uint(f + 25165824.0f); }
-__device__ __forceinline__ uint32_t mbits_div256(float f) { return __float_as_uint(fmaf(f, 0.00390625f, 12582912.0f)); }
-// The constants those bits carry, summed with the level weights 2^(8 (5 - l)) (levels 0..4 and 6:
-// 0x4B400000; level 5, counted twice: 0x4BC00000), modulo 2^64.
-constexpr uint64_t kMagicSum = 0x4B400000ull * ((1ull << 40) + (1ull << 32) + (1ull << 24) + (1ull << 16) + (1ull << 8) + 1ull) +
-                               2ull * 0x4BC00000ull;
 
 // v * 2^T rounded to the nearest f64 (ties to even); below the normal range: signed zero.
 __device__ __forceinline__ double scaled_to_f64(int64_t v, int T) {
@@ -192,84 +212,106 @@ __device__ __forceinline__ void put_digit(const uint64_t (&y)[2 * NA], uint32_t 
     if (lane == 0) mbar_arrive(full);
 }
 
-// Math warps: the tile in buffer b once loaded, its row exponent E (with the row's other column
-// groups, through s_exp and the quad's named barrier) and the thread's 2 NA slices y.
-template <int NA>
+// Math warps: the tile in buffer b once loaded, as the thread's 2 NA biased fixed-point values y.
+template <bool kInF64, int NA>
 __device__ __forceinline__ bool prep_tile(const double2* tiles, uint32_t b, uint32_t& ph_tma, uint32_t mrow,
-                                          const uint32_t* rp, uint32_t (*s_exp)[32 / NA][128], uint32_t cg,
-                                          uint32_t quad, uint32_t row, uint64_t (&y)[2 * NA], uint32_t& E,
+                                          const uint32_t* rp, uint64_t (&y)[2 * NA], uint32_t E, int sigma,
                                           volatile int* abort_flag, int* err, uint64_t* bar_tma, uint32_t* loads_seen) {
-    constexpr uint32_t kCG = 32 / NA;
     if (!wait_or_abort(&bar_tma[b], (ph_tma >> b) & 1u, abort_flag, err)) return false;
     ph_tma ^= 1u << b;
     if (loads_seen) ++loads_seen[b];
     const double2* tile = tiles + (size_t)b * kTileAmps;
-    uint32_t emax = 0;
 #pragma unroll
-    for (int i = 0; i < NA; ++i) {  // first read: the row exponent
+    for (int i = 0; i < NA; ++i) {
         const double2 a = tile[mrow | rp[i]];
-        const uint32_t e0 = (uint32_t)((uint64_t)__double_as_longlong(a.x) >> 52) & 0x7ffu;
-        const uint32_t e1 = (uint32_t)((uint64_t)__double_as_longlong(a.y) >> 52) & 0x7ffu;
-        emax = max(emax, max(e0, e1));
-    }
-    s_exp[b][cg][row] = emax;
-    named_sync(1u + quad, 32u * kCG);
-    E = s_exp[b][0][row];
-#pragma unroll
-    for (uint32_t g = 1; g < kCG; ++g) E = max(E, s_exp[b][g][row]);
-#pragma unroll
-    for (int i = 0; i < NA; ++i) {  // second read: the slices
-        const double2 a = tile[mrow | rp[i]];
-        y[2 * i] = slice(a.x, E);
-        y[2 * i + 1] = slice(a.y, E);
+        if constexpr (kInF64) {
+            y[2 * i] = slice(a.x, E);
+            y[2 * i + 1] = slice(a.y, E);
+        } else {
+            y[2 * i] = renorm(__double_as_longlong(a.x), sigma);
+            y[2 * i + 1] = renorm(__double_as_longlong(a.y), sigma);
+        }
     }
     return true;
 }
 
-// Read back level L of the thread's 2 NA output reals (once digit L's products are done, the last
-// to add to that level) into the 64-bit sums: acc += level x 2^(8 (5 - L)), from the magic-number
-// bits (their constants are removed at the end, modulo 2^64).
-template <int L, int NA>
-__device__ __forceinline__ void read_level(uint64_t (&acc)[2 * NA], uint32_t taddr) {
-    uint32_t v[2 * NA];  // the level's 2 NA columns of this lane, loaded together
+// The level-L columns of this lane (2 NA values, loaded together).
+template <int NA>
+__device__ __forceinline__ void load_level(uint32_t (&v)[2 * NA], uint32_t taddr) {
 #pragma unroll
     for (int part = 0; part < NA / 4; ++part) {
         uint32_t w[8];
-        tmem_ld8(taddr + 64u * (uint32_t)L + 8u * (uint32_t)part, w);
+        tmem_ld8(taddr + 8u * (uint32_t)part, w);
 #pragma unroll
         for (int kk = 0; kk < 8; ++kk) v[8 * part + kk] = w[kk];
     }
+}
+
+// Read back level L (0..5) of the thread's 2 NA output reals, once digit L's products are done (the
+// last to add to that level), into the output sums X' = sum_l L_l 2^(41 - 8 l):
+//   levels 0, 1: V = 256 L0 + L1 (magic-number bits, one 32-bit word);
+//   levels 2, 3: U = 256 L2 + L3, then acc = 2 V 2^32 + U 2^17 (64 bits);
+//   levels 4, 5: acc += L4 2^9 + L5 2 (exact float-to-int conversions: |L| may reach 2^22.5).
+template <int L, int NA>
+__device__ __forceinline__ void read_level(uint64_t (&acc)[2 * NA], uint32_t taddr) {
+    uint32_t v[2 * NA];
+    load_level<NA>(v, taddr + 64u * (uint32_t)L);
     tmem_ld_wait();
 #pragma unroll
     for (int k = 0; k < 2 * NA; ++k) {
         const float f = __uint_as_float(v[k]);
-        if (L == 0) acc[k] = (uint64_t)mbits(f) << 32;
-        else if (L == 1) acc[k] = (uint64_t)((uint32_t)(acc[k] >> 32) * 256u + mbits(f)) << 32;
-        else if (L < 5) acc[k] += (uint64_t)mbits(f) << (8 * (5 - L));
-        else if (L == 5) acc[k] += 2ull * mbits_even(f);
-        else acc[k] += mbits_div256(f);
+        if constexpr (L == 0) {
+            acc[k] = mbits(f);
+        } else if constexpr (L == 1) {
+            acc[k] = (uint32_t)acc[k] * 256u + mbits(f);
+        } else if constexpr (L == 2) {
+            acc[k] = ((uint64_t)mbits(f) << 32) | (uint32_t)acc[k];
+        } else if constexpr (L == 3) {
+            const uint32_t Vm = (uint32_t)acc[k];                                  // V + 257 kMagic
+            const uint32_t Um = (uint32_t)(acc[k] >> 32) * 256u + mbits(f);        // U + 257 kMagic
+            const int32_t V = (int32_t)(Vm - 257u * kMagic), U = (int32_t)(Um - 257u * kMagic);
+            acc[k] = ((uint64_t)(uint32_t)(2 * V) << 32) + (uint64_t)((int64_t)U << 17);
+        } else if constexpr (L == 4) {
+            acc[k] += (uint64_t)((int64_t)__float2int_rn(f) << 9);
+        } else {
+            acc[k] += (uint64_t)((int64_t)__float2int_rn(f) << 1);
+        }
     }
 }
 
-template <int kRegs, int NA>
+// Levels 6 and 7 (level 7 in level 0's columns), once the tile's last products are done:
+// acc += round((256 L6 + L7) 2^-15), rounding half up.
+template <int NA>
+__device__ __forceinline__ void read_levels_67(uint64_t (&acc)[2 * NA], uint32_t taddr) {
+    uint32_t v6[2 * NA], v7[2 * NA];
+    load_level<NA>(v6, taddr + 64u * 6u);
+    load_level<NA>(v7, taddr);
+    tmem_ld_wait();
+#pragma unroll
+    for (int k = 0; k < 2 * NA; ++k) {
+        const int32_t R = __float2int_rn(__uint_as_float(v6[k])) * 256 + __float2int_rn(__uint_as_float(v7[k]));
+        acc[k] += (uint64_t)(int64_t)((R + 16384) >> 15);
+    }
+}
+
+template <int kRegs, int NA, bool kInF64, bool kOutF64>
 __global__ void __maxnreg__(kRegs)
     tensor64_pass_kernel(double2* __restrict__ psi, const unsigned char* __restrict__ wts,
                          const __grid_constant__ TPassParams P, int* __restrict__ err) {
     using LY = Layout<NA>;
     constexpr uint32_t kNT = LY::kNT, kMathWarps = LY::kMathWarps, kMmaWarp = LY::kMmaWarp, kTmaWarp = LY::kTmaWarp;
-    constexpr uint32_t kCG = LY::kCG;
     extern __shared__ __align__(1024) unsigned char smem[];
     double2* tiles = reinterpret_cast<double2*>(smem);  // two tile buffers
     unsigned char* w_sm = smem + 2 * (size_t)kTileAmps * 16;
     __shared__ uint64_t seg_off[1u << (kTQ - kLowQ)];
     __shared__ uint32_t mpos[128];
     __shared__ uint32_t rpos[32];
-    __shared__ uint32_t s_exp[2][kCG][128];
     __shared__ __align__(8) uint64_t bar_tma[2];      // tile loaded into buffer b (TMA bytes)
-    __shared__ __align__(8) uint64_t bar_written[2];  // tile results written to buffer b (16 math warps)
-    __shared__ __align__(8) uint64_t bar_full[2];     // operand slot holds the next digit (16 math warps)
+    __shared__ __align__(8) uint64_t bar_written[2];  // tile results written to buffer b (math warps)
+    __shared__ __align__(8) uint64_t bar_full[2];     // operand slot holds the next digit (math warps)
     __shared__ __align__(8) uint64_t bar_mma[2];      // that digit's MMAs are done (commit)
-    __shared__ __align__(8) uint64_t bar_acc;         // accumulators read back (16 math warps)
+    __shared__ __align__(8) uint64_t bar_acc;         // accumulators read back (math warps)
+    __shared__ __align__(8) uint64_t bar_l0;          // level 0 read back: its columns take level 7
     __shared__ uint32_t tmem_base;
     __shared__ int s_abort;
     __shared__ uint32_t s_loads[2], s_loads_seen[2], s_commits[2], s_commits_seen[2];
@@ -277,6 +319,22 @@ __global__ void __maxnreg__(kRegs)
     const uint32_t c = P.c;
     const uint32_t nseg = 1u << (kTQ - c);
     const uint32_t seg_amps = 1u << c;
+
+    // the register scale this pass reads and the one it writes
+    const ScaleSlot in = P.slots[P.cur];
+    uint32_t E = 0;
+    int sigma = 0, S_in;
+    if constexpr (kInF64) {
+        E = in.mag;
+        S_in = 1075 - (int)E;
+    } else {
+        sigma = in.mag ? kTopBits - 32 - (32 - __clz((int)in.mag)) : 0;
+        S_in = in.S + sigma;
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+        P.slots[(P.cur + 1) % 3].S = S_in;
+        P.slots[(P.cur + 2) % 3].mag = 0;
+    }
 
     for (uint32_t s = tid; s < nseg; s += kNT) {
         uint64_t off = 0;
@@ -319,6 +377,7 @@ __global__ void __maxnreg__(kRegs)
             s_loads[i] = s_loads_seen[i] = s_commits[i] = s_commits_seen[i] = 0;
         }
         mbar_init(&bar_acc, kMathWarps);
+        mbar_init(&bar_l0, kMathWarps);
         s_abort = 0;
         fence_mbar_init();
     }
@@ -372,9 +431,10 @@ __global__ void __maxnreg__(kRegs)
         bulk_wait_all();
     } else if (warp == kMmaWarp) {
         // ---- MMA issue: digit s of a tile once its slot is full (and, for digit 0, once the
-        // previous tile's accumulators have been read back) ----
+        // previous tile's accumulators have been read back; for the level-7 products, once this
+        // tile's level 0 has been) ----
         const uint32_t w_addr = smem_addr(w_sm);
-        uint32_t ph_full = 0, ph_acc = 0;  // phase parities, bit = slot
+        uint32_t ph_full = 0, ph_acc = 0, ph_l0 = 0;  // phase parities, bit = slot
         bool ok = true;
         for (uint32_t i = 0; ok && i < my_tiles; ++i) {
 #pragma unroll
@@ -386,9 +446,9 @@ __global__ void __maxnreg__(kRegs)
                 }
                 if (ok) ok = wait_or_abort(&bar_full[slot], (ph_full >> slot) & 1u, abort_flag, err);
                 ph_full ^= 1u << slot;
+                const uint32_t a_tm = tmem + kSlotCol + 32u * slot;
                 if (ok && lane == 0) {
                     tc_after_sync();
-                    const uint32_t a_tm = tmem + kSlotCol + 32u * slot;
 #pragma unroll
                     for (int tt = 0; tt + s < kDigits; ++tt) {
                         const uint32_t d_tm = tmem + 64u * (uint32_t)(s + tt);
@@ -398,6 +458,22 @@ __global__ void __maxnreg__(kRegs)
                             mma_f16_ta(d_tm, a_tm + 8u * ks, smem_desc(wb + 256u * ks, 128u, 1024u),
                                        (s > 0 || ks > 0) ? 1u : 0u);
                     }
+                }
+                if (s >= 1) {
+                    if (ok && s == 1) {
+                        ok = wait_or_abort(&bar_l0, ph_l0, abort_flag, err);
+                        ph_l0 ^= 1u;
+                    }
+                    if (ok && lane == 0) {
+                        tc_after_sync();
+                        const uint32_t wb = w_addr + (uint32_t)(kDigits - s) * kWDigitBytes;  // pair (s, 7 - s)
+#pragma unroll
+                        for (uint32_t ks = 0; ks < 4; ++ks)
+                            mma_f16_ta(tmem, a_tm + 8u * ks, smem_desc(wb + 256u * ks, 128u, 1024u),
+                                       (s > 1 || ks > 0) ? 1u : 0u);
+                    }
+                }
+                if (ok && lane == 0) {
                     mma_commit(&bar_mma[slot]);
                     ++s_commits[slot];
                 }
@@ -410,13 +486,12 @@ __global__ void __maxnreg__(kRegs)
         const uint32_t row = 32u * quad + lane;
         const uint32_t lane_addr = (32u * quad) << 16;
         const uint32_t slot0 = tmem + lane_addr + kSlotCol + (uint32_t)NA * cg;
-        const int32_t* w_exp = reinterpret_cast<const int32_t*>(w_sm + kDigits * kWDigitBytes) + 2u * NA * cg;
         const uint32_t* rp = rpos + (uint32_t)NA * cg;
         const uint32_t mrow = mpos[row];  // amplitude i of this thread sits at mrow | rp[i]
         const bool counter = quad == 0 && cg == 0 && lane == 0;
         uint32_t ph_tma = 0, ph_mma = 0;  // phase parities, bit = buffer / slot
+        uint32_t mag = 0;                 // OR of the fixed-point outputs' high-word magnitudes
         uint64_t y[2 * NA];
-        uint32_t E = 0;
         auto wait_mma = [&](uint32_t slot) -> bool {
             const bool r = wait_or_abort(&bar_mma[slot], (ph_mma >> slot) & 1u, abort_flag, err);
             ph_mma ^= 1u << slot;
@@ -424,8 +499,8 @@ __global__ void __maxnreg__(kRegs)
             tc_after_sync();
             return r;
         };
-        bool ok = my_tiles > 0 && prep_tile<NA>(tiles, 0, ph_tma, mrow, rp, s_exp, cg, quad, row, y, E, abort_flag, err,
-                                            bar_tma, counter ? s_loads_seen : nullptr);
+        bool ok = my_tiles > 0 && prep_tile<kInF64, NA>(tiles, 0, ph_tma, mrow, rp, y, E, sigma, abort_flag, err,
+                                                        bar_tma, counter ? s_loads_seen : nullptr);
         if (ok) {
             put_digit<0, NA>(y, slot0, &bar_full[0], lane);
             put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
@@ -439,6 +514,9 @@ __global__ void __maxnreg__(kRegs)
             ok = wait_mma(0);
             if (ok) {
                 read_level<0, NA>(acc, acc_addr);
+                tc_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&bar_l0);  // level 0's columns now take level 7
                 put_digit<2, NA>(y, slot0, &bar_full[0], lane);
                 ok = wait_mma(1);
             }
@@ -463,34 +541,43 @@ __global__ void __maxnreg__(kRegs)
             }
             if (!ok) break;
             // the next tile's slices while this tile's last digits multiply
-            const uint32_t E_this = E;
             const bool has_next = i + 1 < my_tiles;
             if (has_next)
-                ok = prep_tile<NA>(tiles, b ^ 1u, ph_tma, mrow, rp, s_exp, cg, quad, row, y, E, abort_flag, err, bar_tma,
-                                   counter ? s_loads_seen : nullptr);
-            // levels 5 and 6: the commits of digits 5 (slot 1) and 6 (slot 0), the last of this tile
+                ok = prep_tile<kInF64, NA>(tiles, b ^ 1u, ph_tma, mrow, rp, y, E, sigma, abort_flag, err, bar_tma,
+                                           counter ? s_loads_seen : nullptr);
+            // levels 5, 6 and 7: the commits of digits 5 (slot 1) and 6 (slot 0), the last of this tile
             const bool done5 = wait_mma(1);
             if (done5) read_level<5, NA>(acc, acc_addr);
             const bool done6 = wait_mma(0);
             if (!(done5 && done6)) break;
-            read_level<6, NA>(acc, acc_addr);
+            read_levels_67<NA>(acc, acc_addr);
             tc_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive(&bar_acc);
-            // the next tile's first two digits go in while this tile's results are rounded
+            // the next tile's first two digits go in while this tile's results are written
             if (has_next && ok) {
                 put_digit<0, NA>(y, slot0, &bar_full[0], lane);
                 put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
             }
             double2* tile = tiles + (size_t)b * kTileAmps;
 #pragma unroll
-            for (int k = 0; k < NA; ++k)
-                tile[mrow | rp[k]] =
-                    make_double2(scaled_to_f64((int64_t)(acc[2 * k] - kMagicSum), (int)E_this + w_exp[2 * k] - 2094),
-                                 scaled_to_f64((int64_t)(acc[2 * k + 1] - kMagicSum), (int)E_this + w_exp[2 * k + 1] - 2094));
+            for (int k = 0; k < NA; ++k) {
+                const int64_t v0 = (int64_t)acc[2 * k], v1 = (int64_t)acc[2 * k + 1];
+                if constexpr (kOutF64) {
+                    tile[mrow | rp[k]] = make_double2(scaled_to_f64(v0, -S_in), scaled_to_f64(v1, -S_in));
+                } else {
+                    const int32_t h0 = (int32_t)(v0 >> 32), h1 = (int32_t)(v1 >> 32);
+                    mag |= (uint32_t)(h0 ^ (h0 >> 31)) | (uint32_t)(h1 ^ (h1 >> 31));
+                    tile[mrow | rp[k]] = make_double2(__longlong_as_double(v0), __longlong_as_double(v1));
+                }
+            }
             fence_proxy_async();  // the results are read by the TMA store
             __syncwarp();
             if (lane == 0) mbar_arrive(&bar_written[b]);
+        }
+        if constexpr (!kOutF64) {
+            mag = __reduce_or_sync(0xffffffffu, mag);
+            if (lane == 0 && mag) atomicOr(&P.slots[(P.cur + 1) % 3].mag, mag);
         }
     }
     // teardown: after an abort, let the copies and MMAs in flight land before the memory goes away
@@ -509,6 +596,20 @@ __global__ void __maxnreg__(kRegs)
     if (warp == 0) tmem_dealloc(tmem_base, 512);
 }
 
+// The largest biased f64 exponent of the register's components, into slot 0 of its scale ring (the
+// ring cleared before).
+__global__ void tensor64_maxexp_kernel(const double2* __restrict__ psi, uint64_t len, ScaleSlot* slots) {
+    uint32_t m = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 a = psi[i];
+        const uint32_t e0 = (uint32_t)((uint64_t)__double_as_longlong(a.x) >> 52) & 0x7ffu;
+        const uint32_t e1 = (uint32_t)((uint64_t)__double_as_longlong(a.y) >> 52) & 0x7ffu;
+        m = max(m, max(e0, e1));
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31u) == 0 && m) atomicMax(&slots[0].mag, m);
+}
+
 // ---- host -----------------------------------------------------------------------------------------
 uint16_t fp16_of_small_int(int d) {  // exact for |d| <= 2048
     if (d == 0) return 0;
@@ -519,19 +620,19 @@ uint16_t fp16_of_small_int(int d) {  // exact for |d| <= 2048
     return (uint16_t)(sgn | ((uint32_t)(e + 15) << 10) | mant);
 }
 
-// fp16 bits of the digit byte c - 128, for every byte c.
+// fp16 bits of the balanced digits -128 .. 128.
 struct DigitTable {
-    uint16_t h[256];
+    uint16_t h[257];
     DigitTable() {
-        for (int c = 0; c < 256; ++c) h[c] = fp16_of_small_int(c - 128);
+        for (int d = -128; d <= 128; ++d) h[d + 128] = fp16_of_small_int(d);
     }
 };
 
 // A block's weights: the real 64 x 64 form W[2r' + c'][2r + c] = ((Re, -Im), (Im, Re)) of U[r'][r]
-// (row = output real, column = input real); per row its largest exponent F, the 53-bit integers
-// round(W * 2^(1075 - F)) and their seven balanced base-256 digits as fp16 in the operand layout
-// (digit t = 0 most significant), then the 64 row exponents.
-void block_weights64(const dense::Block& b, unsigned char* out) {
+// (row = output real, column = input real) as the integers round(W 2^55) and their seven balanced
+// base-256 digits (|digit| <= 128; digit t = 0 most significant) in fp16, in the operand layout.
+// False when an entry is not finite or above 1 in magnitude (the digit bounds assume a unitary).
+bool block_weights64(const dense::Block& b, unsigned char* out) {
     static const DigitTable digits;
     static thread_local double W[64][64];
     for (uint32_t rp = 0; rp < 32; ++rp)
@@ -543,25 +644,21 @@ void block_weights64(const dense::Block& b, unsigned char* out) {
             W[2 * rp + 1][2 * r + 1] = u.re;
         }
     uint16_t* dig = reinterpret_cast<uint16_t*>(out);
-    int32_t* F = reinterpret_cast<int32_t*>(out + kDigits * kWDigitBytes);
-    for (uint32_t n = 0; n < 64; ++n) {
-        int fmax = 0;
+    for (uint32_t n = 0; n < 64; ++n)
         for (uint32_t k = 0; k < 64; ++k) {
-            uint64_t bits;
-            memcpy(&bits, &W[n][k], 8);
-            fmax = std::max(fmax, (int)((bits >> 52) & 0x7ff));
-        }
-        F[n] = fmax;
-        for (uint32_t k = 0; k < 64; ++k) {
-            int64_t X = 0;
-            uint64_t bits;
-            memcpy(&bits, &W[n][k], 8);
-            if (fmax > 0 && ((bits >> 52) & 0x7ff) != 0) X = std::llrint(std::ldexp(W[n][k], 1075 - fmax));
-            const uint64_t Y = (uint64_t)X + kBias;
+            const double w = W[n][k];
+            if (!(std::fabs(w) <= 1.0 + 1e-9)) return false;
+            int64_t rest = std::llrint(std::ldexp(w, kWScale));
+            int d[kDigits];
+            for (int t = kDigits - 1; t >= 1; --t) {
+                d[t] = (int)((((rest + 128) % 256) + 256) % 256) - 128;
+                rest = (rest - d[t]) / 256;
+            }
+            d[0] = (int)rest;  // |d[0]| <= 128
             for (int t = 0; t < kDigits; ++t)
-                dig[(size_t)t * (kWDigitBytes / 2) + w_off16(n, k)] = digits.h[(Y >> (8 * (6 - t))) & 0xffu];
+                dig[(size_t)t * (kWDigitBytes / 2) + w_off16(n, k)] = digits.h[std::clamp(d[t], -128, 128) + 128];
         }
-    }
+    return true;
 }
 
 // A gate goes through dense blocks when each of its dense factors (the multi-bit X/Y/Z/S/T split
@@ -586,52 +683,78 @@ int plan_blocks(const qvnt_gate* gates, size_t count, uint32_t L, std::vector<de
 }
 
 using PassFn = void (*)(double2*, const unsigned char*, const TPassParams, int*);
+// The four forms of one layout, indexed by (input f64) * 2 + (output f64).
 struct PassKernel {
-    PassFn fn = nullptr;
+    PassFn fn[4] = {nullptr, nullptr, nullptr, nullptr};
     uint32_t threads = 0;
     int regs = 0;
     char why[160] = {0};
 };
 
-// The kernel builds in order of preference (measured on a 30-qubit pass: 17.1 ms against 20.3 ms):
-// 16 math warps of 8 amplitudes with 96 registers (five of the eighteen warps share an SM
-// sub-partition's 16K registers), 8 math warps of 16 amplitudes with 168 registers (three of ten);
-// QVNT_T64_LAYOUT=8 or 16 picks one (amplitudes per math thread).
-PassKernel pick_kernel() {
+template <int kRegs, int NA>
+PassKernel forms_of() {
     PassKernel k;
+    k.fn[0] = tensor64_pass_kernel<kRegs, NA, false, false>;
+    k.fn[1] = tensor64_pass_kernel<kRegs, NA, false, true>;
+    k.fn[2] = tensor64_pass_kernel<kRegs, NA, true, false>;
+    k.fn[3] = tensor64_pass_kernel<kRegs, NA, true, true>;
+    k.threads = Layout<NA>::kNT;
+    return k;
+}
+
+// The layouts in order of preference (measured on a 30-qubit pass of the earlier per-row-exponent
+// form: 17.1 ms against 20.3 ms): 16 math warps of 8 amplitudes with 96 registers (five of the
+// eighteen warps share an SM sub-partition's 16K registers), 8 math warps of 16 amplitudes with 168
+// registers (three of ten); QVNT_T64_LAYOUT=8 or 16 picks one (amplitudes per math thread).
+PassKernel pick_kernel() {
+    PassKernel out;
     struct Cand {
-        PassFn fn;
-        uint32_t threads;
+        PassKernel k;
         int na;
     };
-    const Cand cands[3] = {{tensor64_pass_kernel<96, 8>, Layout<8>::kNT, 8},
-                           {tensor64_pass_kernel<168, 16>, Layout<16>::kNT, 16},
-                           {tensor64_pass_kernel<128, 16>, Layout<16>::kNT, 16}};
+    const Cand cands[2] = {{forms_of<96, 8>(), 8}, {forms_of<168, 16>(), 16}};
     const char* env = std::getenv("QVNT_T64_LAYOUT");
     const int want = env ? std::atoi(env) : 0;
     for (const Cand& c : cands) {
         if (want && c.na != want) continue;
-        cudaFuncAttributes a;
-        if (cudaFuncGetAttributes(&a, (const void*)c.fn) != cudaSuccess) continue;
-        if (a.maxThreadsPerBlock < (int)c.threads) {
-            snprintf(k.why, sizeof k.why, "%d registers allow %d threads per block, %u needed", a.numRegs,
-                     a.maxThreadsPerBlock, c.threads);
-            continue;
+        bool good = true;
+        int regs = 0;
+        for (PassFn fn : c.k.fn) {
+            cudaFuncAttributes a;
+            if (cudaFuncGetAttributes(&a, (const void*)fn) != cudaSuccess) {
+                good = false;
+                break;
+            }
+            if (a.maxThreadsPerBlock < (int)c.k.threads) {
+                snprintf(out.why, sizeof out.why, "%d registers allow %d threads per block, %u needed", a.numRegs,
+                         a.maxThreadsPerBlock, c.k.threads);
+                good = false;
+                break;
+            }
+            if (cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDyn) !=
+                cudaSuccess) {
+                snprintf(out.why, sizeof out.why, "shared-memory attribute refused");
+                good = false;
+                break;
+            }
+            regs = std::max(regs, a.numRegs);
         }
-        if (cudaFuncSetAttribute((const void*)c.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDyn) !=
-            cudaSuccess) {
-            snprintf(k.why, sizeof k.why, "shared-memory attribute refused");
-            continue;
-        }
-        k.fn = c.fn;
-        k.threads = c.threads;
-        k.regs = a.numRegs;
-        return k;
+        if (!good) continue;
+        out = c.k;
+        out.regs = regs;
+        return out;
     }
     cudaGetLastError();
-    return k;
+    return out;
 }
 
+// The register's scale ring: three slots after the 64 bytes of device results.
+ScaleSlot* scale_ring(qvnt_reg* r) {
+    return reinterpret_cast<ScaleSlot*>(reinterpret_cast<char*>(r->d_small) + 64);
+}
+
+// One run of blockable gates: the reduction for the register's largest exponent, then one pass per
+// block (f64 in for the first, f64 out for the last, 64-bit block floating point in between).
 int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     const uint32_t L = (uint32_t)__builtin_ctzll(r->len);
     std::vector<dense::Block> blocks;
@@ -642,12 +765,22 @@ int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     EngineBuffers& fs = r->bufs;
     TRY_T(fs.acquire(wbytes, r->stream));
     unsigned char* hw = static_cast<unsigned char*>(fs.h_buf);
-    for (size_t i = 0; i < blocks.size(); ++i) block_weights64(blocks[i], hw + i * (size_t)kWBlockBytes);
+    for (size_t i = 0; i < blocks.size(); ++i)
+        if (!block_weights64(blocks[i], hw + i * (size_t)kWBlockBytes)) return apply_plain(r, gates, count);
     TRY_T(fs.upload(wbytes, r->stream));
     static const PassKernel kern = pick_kernel();
-    if (!kern.fn) return set_error(QVNT_ERR_CUDA, "tensor64 kernel: %s", kern.why);
+    if (!kern.fn[0]) return set_error(QVNT_ERR_CUDA, "tensor64 kernel: %s", kern.why);
     int* d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(r->d_small) + 32);
-    for (const dense::PPlan& p : passes) {
+    ScaleSlot* ring = scale_ring(r);
+    QVNT_CUDA_TRY(cudaMemsetAsync(ring, 0, 3 * sizeof(ScaleSlot), r->stream));
+    {
+        const uint64_t grid = std::min<uint64_t>((uint64_t)r->ctx->geo.sms * 4, (r->len + 255) / 256);
+        tensor64_maxexp_kernel<<<(unsigned)grid, 256, 0, r->stream>>>(r->psi, r->len, ring);
+        QVNT_CUDA_TRY(cudaGetLastError());
+        r->launches += 1;
+    }
+    for (size_t pi = 0; pi < passes.size(); ++pi) {
+        const dense::PPlan& p = passes[pi];
         TPassParams P;
         memset(&P, 0, sizeof P);
         uint32_t n = 0, pos_of[64];
@@ -668,12 +801,15 @@ int run_blocks(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
         for (uint32_t q = 0; q < L; ++q)
             if ((blk.sup >> q) & 1ull) P.bits[jj++] = (uint8_t)pos_of[q];
         P.w_off = bi * (uint64_t)kWBlockBytes;
+        P.slots = ring;
+        P.cur = (uint32_t)(pi % 3);
+        const int form = (pi == 0 ? 2 : 0) + (pi + 1 == passes.size() ? 1 : 0);
         // persistent (one CTA per SM), or one CTA per tile for registers that share the GPU
         const uint64_t grid = r->tile_grid ? P.ntiles : std::min<uint64_t>((uint64_t)r->ctx->geo.sms, P.ntiles);
         cudaEvent_t stop = nullptr;
         TRY_T(timing_begin(r, &stop));
-        kern.fn<<<(unsigned)grid, kern.threads, kSmemDyn, r->stream>>>(r->psi, static_cast<const unsigned char*>(fs.d_buf), P,
-                                                               d_err);
+        kern.fn[form]<<<(unsigned)grid, kern.threads, kSmemDyn, r->stream>>>(
+            r->psi, static_cast<const unsigned char*>(fs.d_buf), P, d_err);
         const cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess)
             return set_error(QVNT_ERR_CUDA, "tensor64 launch (%d threads, %zu B dynamic shared memory, %d registers): %s",
@@ -704,7 +840,6 @@ int apply_tensor64(qvnt_reg* r, const qvnt_gate* gates, size_t count) {
     }
     return QVNT_OK;
 }
-
 int tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* plain_gates) {
     uint64_t np = 0, pg = 0;
     if (L < (uint32_t)kTQ) {
