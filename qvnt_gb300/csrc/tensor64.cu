@@ -16,13 +16,15 @@
 // column = input component) is held as round(W 2^55), |.| <= 2^55; it and the state are split into
 // seven balanced base-256 digits (|digit| <= 128), exact in fp16.  The product is the sum over digit
 // pairs (s, t) of A_s B_t^T weighted by 2^(96 - 8 (s + t)); the 34 pairs with s + t <= 7 are issued as
-// tcgen05.mma kind::f16 (M = 128 rows, N = 64, K = 16) into eight FP32 accumulators in tensor memory,
-// one per level l = s + t.  Every partial sum is an integer below 2^23 in magnitude (at most 7 products
+// tcgen05.mma kind::f16 (M = 128 rows, K = 16) into eight FP32 accumulators in tensor memory, one per
+// level l = s + t (the pairs of one digit s into adjacent levels as one MMA of N = 64 m, m <= 4: 12
+// MMAs per K step instead of 34; an MMA costs about the same for any N up to 256).  Every partial sum is an integer below 2^23 in magnitude (at most 7 products
 // of 64 terms of |digit product| <= 2^14, those with a top digit smaller), so the FP32 accumulation is
 // exact.  Levels >= 8 are dropped (2^-23 of an output unit per level-8 unit: typically 0.01 unit).
 // The accumulators are read back (tcgen05.ld), turned into integers (a magic-number add below 2^22,
 // an exact float-to-int conversion above), and combined into the output X' = sum_l L_l 2^(41 - 8 l)
-// with one rounding (of the levels 6 and 7 part); no FP64 instruction is issued.
+// with one rounding (of the levels 6 and 7 part, to within 1/2 + 2^-9 of a unit); no FP64
+// instruction is issued.
 //
 // Kernel (one pass = one block): persistent CTAs, one per SM (tensor memory: all 512 columns), of
 // 18 warps (10 in the 16-amplitude layout) in three roles synchronised by mbarriers only.  Per tile of
@@ -35,9 +37,9 @@
 //     eight levels and the output;
 //   * the MMA warp issues each digit's products once its slot is full and commits them to the
 //     slot's mbarrier.
-// Level l is final once digit l's products are done; level 7 accumulates in level 0's columns, which
-// the math warps release right after reading level 0.  The next tile is sliced while this tile's last
-// digits multiply, and this tile's results are written while the next tile's first digits multiply.
+// Level l is final once digit l's products are done; level 0 sits in level 7's columns, which the
+// math warps clear right after reading level 0.  The next tile is read once this tile's levels
+// are, and this tile's results are written while the next tile's first digits multiply.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -83,13 +85,21 @@ constexpr int kTopBits = 54;                    // fixed-point inputs are renorm
 constexpr uint32_t kWDigitBytes = 64 * 64 * 2;  // one fp16 digit matrix of a block (8 KB)
 constexpr uint32_t kWBlockBytes = kDigits * kWDigitBytes;
 constexpr uint32_t kWaitLimit = 1u << 22;       // mbarrier polls before a wait gives up
-constexpr uint32_t kSlotCol = 448;              // tensor-memory columns: levels 0..6 at 64 l, slots 448 / 480
+constexpr uint32_t kSlotCol = 448;              // tensor-memory columns of the two operand slots (448, 480)
+// Tensor-memory column of level l's accumulator: levels 1..7 side by side from column 0 (so that the
+// pairs of one digit s >= 1, levels s .. 7, are adjacent), level 0 in level 7's columns (level 0 is
+// read back and its columns cleared before the first level-7 product).
+__host__ __device__ constexpr uint32_t level_col(int l) { return l == 0 ? 384u : 64u * (uint32_t)(l - 1); }
 constexpr uint64_t kBias = 0x80808080808080ull; // 128 in each of the 7 digit bytes
 constexpr uint32_t kMagic = 0x4B400000u;        // bits of 1.5 * 2^23
 constexpr size_t kSmemDyn = 2 * (size_t)kTileAmps * 16 + kWBlockBytes;
 
-// Instruction descriptor of kind::f16: FP32 accumulator, A and B fp16 and K-major, N = 64, M = 128.
-constexpr uint32_t kIdesc16 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+// Instruction descriptor of kind::f16: FP32 accumulator, A and B fp16 and K-major, M = 128, N = 64 m
+// (m levels side by side: m digit matrices of a block, stacked 8 KB apart, are one operand of 64 m
+// rows in the shared-memory layout below).
+__host__ __device__ constexpr uint32_t idesc16(uint32_t m) {
+    return (1u << 4) | (((64u * m) >> 3) << 17) | ((128u >> 4) << 24);
+}
 
 // fp16 element offset of B[row][k] (row = output real, k = input real) in the no-swizzle K-major
 // operand layout: core matrices of 8 rows x 16 bytes; adjacent along K 128 B apart, 8-row groups
@@ -118,12 +128,13 @@ struct TPassParams {
     uint8_t bits[dense::kBQ];  // tile-local bit of block bit j
 };
 
-__device__ __forceinline__ void mma_f16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_f16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                           uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "r"(a_tmem), "l"(b), "r"(kIdesc16), "r"(accumulate)
+        "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 
@@ -255,7 +266,7 @@ __device__ __forceinline__ void load_level(uint32_t (&v)[2 * NA], uint32_t taddr
 template <int L, int NA>
 __device__ __forceinline__ void read_level(uint64_t (&acc)[2 * NA], uint32_t taddr) {
     uint32_t v[2 * NA];
-    load_level<NA>(v, taddr + 64u * (uint32_t)L);
+    load_level<NA>(v, taddr + level_col(L));
     tmem_ld_wait();
 #pragma unroll
     for (int k = 0; k < 2 * NA; ++k) {
@@ -280,17 +291,18 @@ __device__ __forceinline__ void read_level(uint64_t (&acc)[2 * NA], uint32_t tad
 }
 
 // Levels 6 and 7 (level 7 in level 0's columns), once the tile's last products are done:
-// acc += round((256 L6 + L7) 2^-15), rounding half up.
+// acc += round(L6 2^-7 + L7 2^-15): the sum taken in FP32 (|.| < 2^16, so one rounding of at most
+// 2^-9), then rounded to the nearest integer by a magic-number add: within 1/2 + 2^-9 of a unit.
 template <int NA>
 __device__ __forceinline__ void read_levels_67(uint64_t (&acc)[2 * NA], uint32_t taddr) {
     uint32_t v6[2 * NA], v7[2 * NA];
-    load_level<NA>(v6, taddr + 64u * 6u);
-    load_level<NA>(v7, taddr);
+    load_level<NA>(v6, taddr + level_col(6));
+    load_level<NA>(v7, taddr + level_col(7));
     tmem_ld_wait();
 #pragma unroll
     for (int k = 0; k < 2 * NA; ++k) {
-        const int32_t R = __float2int_rn(__uint_as_float(v6[k])) * 256 + __float2int_rn(__uint_as_float(v7[k]));
-        acc[k] += (uint64_t)(int64_t)((R + 16384) >> 15);
+        const float t = fmaf(__uint_as_float(v6[k]), 0.0078125f, __uint_as_float(v7[k]) * 3.0517578125e-05f);
+        acc[k] += (uint64_t)(int64_t)(int32_t)(mbits(t) - kMagic);
     }
 }
 
@@ -447,31 +459,33 @@ __global__ void __maxnreg__(kRegs)
                 if (ok) ok = wait_or_abort(&bar_full[slot], (ph_full >> slot) & 1u, abort_flag, err);
                 ph_full ^= 1u << slot;
                 const uint32_t a_tm = tmem + kSlotCol + 32u * slot;
+                // the pairs (s, t0 .. t0 + m - 1) into m adjacent levels from s + t0: one MMA of N = 64 m per
+                // K step (the block's digit matrices t0 .. t0 + m - 1 are one operand of 64 m rows)
+                auto issue = [&](int t0, int m, bool init) {
+                    const uint32_t d_tm = tmem + level_col(s + t0);
+                    const uint32_t wb = w_addr + (uint32_t)t0 * kWDigitBytes;
+#pragma unroll
+                    for (uint32_t ks = 0; ks < 4; ++ks)
+                        mma_f16_ta(d_tm, a_tm + 8u * ks, smem_desc(wb + 256u * ks, 128u, 1024u), idesc16((uint32_t)m),
+                                   (init && ks == 0) ? 0u : 1u);
+                };
                 if (ok && lane == 0) {
                     tc_after_sync();
-#pragma unroll
-                    for (int tt = 0; tt + s < kDigits; ++tt) {
-                        const uint32_t d_tm = tmem + 64u * (uint32_t)(s + tt);
-                        const uint32_t wb = w_addr + (uint32_t)tt * kWDigitBytes;
-#pragma unroll
-                        for (uint32_t ks = 0; ks < 4; ++ks)
-                            mma_f16_ta(d_tm, a_tm + 8u * ks, smem_desc(wb + 256u * ks, 128u, 1024u),
-                                       (s > 0 || ks > 0) ? 1u : 0u);
+                    if (s == 0) {  // levels 1..4, 5..6, then level 0 (its own columns)
+                        issue(1, 4, true);
+                        issue(5, 2, true);
+                        issue(0, 1, true);
+                    } else {       // levels s .. 7; for digit 1, levels 5..7 once level 0 is read and cleared
+                        issue(0, min(4, 8 - s), false);
                     }
                 }
-                if (s >= 1) {
-                    if (ok && s == 1) {
-                        ok = wait_or_abort(&bar_l0, ph_l0, abort_flag, err);
-                        ph_l0 ^= 1u;
-                    }
-                    if (ok && lane == 0) {
-                        tc_after_sync();
-                        const uint32_t wb = w_addr + (uint32_t)(kDigits - s) * kWDigitBytes;  // pair (s, 7 - s)
-#pragma unroll
-                        for (uint32_t ks = 0; ks < 4; ++ks)
-                            mma_f16_ta(tmem, a_tm + 8u * ks, smem_desc(wb + 256u * ks, 128u, 1024u),
-                                       (s > 1 || ks > 0) ? 1u : 0u);
-                    }
+                if (s == 1 && ok) {
+                    ok = wait_or_abort(&bar_l0, ph_l0, abort_flag, err);
+                    ph_l0 ^= 1u;
+                }
+                if (ok && lane == 0 && s > 0 && 8 - s > 4) {
+                    tc_after_sync();
+                    issue(4, 4 - s, false);
                 }
                 if (ok && lane == 0) {
                     mma_commit(&bar_mma[slot]);
@@ -505,7 +519,7 @@ __global__ void __maxnreg__(kRegs)
             put_digit<0, NA>(y, slot0, &bar_full[0], lane);
             put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
         }
-        const uint32_t acc_addr = tmem + lane_addr + 2u * NA * cg;  // this thread's columns of level 0
+        const uint32_t acc_addr = tmem + lane_addr + 2u * NA * cg;  // this thread's columns at column 0
         for (uint32_t i = 0; ok && i < my_tiles; ++i) {
             const uint32_t b = i & 1u;
             // a slot takes digit s once the MMAs of digit s - 2 are done; level l is final once digit
@@ -514,9 +528,15 @@ __global__ void __maxnreg__(kRegs)
             ok = wait_mma(0);
             if (ok) {
                 read_level<0, NA>(acc, acc_addr);
+                {  // level 0's columns, cleared, take level 7
+                    uint32_t z[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+                    for (int part = 0; part < NA / 4; ++part) tmem_st8(acc_addr + level_col(7) + 8u * part, z);
+                    tmem_st_wait();
+                }
                 tc_before_sync();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&bar_l0);  // level 0's columns now take level 7
+                if (lane == 0) mbar_arrive(&bar_l0);
                 put_digit<2, NA>(y, slot0, &bar_full[0], lane);
                 ok = wait_mma(1);
             }
@@ -540,11 +560,6 @@ __global__ void __maxnreg__(kRegs)
                 put_digit<6, NA>(y, slot0, &bar_full[0], lane);
             }
             if (!ok) break;
-            // the next tile's slices while this tile's last digits multiply
-            const bool has_next = i + 1 < my_tiles;
-            if (has_next)
-                ok = prep_tile<kInF64, NA>(tiles, b ^ 1u, ph_tma, mrow, rp, y, E, sigma, abort_flag, err, bar_tma,
-                                           counter ? s_loads_seen : nullptr);
             // levels 5, 6 and 7: the commits of digits 5 (slot 1) and 6 (slot 0), the last of this tile
             const bool done5 = wait_mma(1);
             if (done5) read_level<5, NA>(acc, acc_addr);
@@ -554,7 +569,12 @@ __global__ void __maxnreg__(kRegs)
             tc_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive(&bar_acc);
-            // the next tile's first two digits go in while this tile's results are written
+            // the next tile (its load had the whole of this tile to land: the buffer's previous tile is
+            // stored first) and its first two digits, while this tile's results are written
+            const bool has_next = i + 1 < my_tiles;
+            if (has_next)
+                ok = prep_tile<kInF64, NA>(tiles, b ^ 1u, ph_tma, mrow, rp, y, E, sigma, abort_flag, err, bar_tma,
+                                           counter ? s_loads_seen : nullptr);
             if (has_next && ok) {
                 put_digit<0, NA>(y, slot0, &bar_full[0], lane);
                 put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
