@@ -30,7 +30,8 @@
 // 18 warps (10 in the 16-amplitude layout) in three roles synchronised by mbarriers only.  Per tile of
 // 4096 amplitudes (12 tile qubits: the 7 lowest, so a tile is 2 KB runs, plus the block's):
 //   * the copy warp keeps two shared-memory tile buffers filled with TMA bulk loads and stores each
-//     tile once its results are written;
+//     tile once its results are written (into the other buffer, whose tile was sliced just before:
+//     a buffer is reloaded more than a tile ahead of its use);
 //   * 16 math warps each take one operand row (lane quadrant) and 8 of its 32 amplitudes (or 8 warps
 //     and 16 amplitudes): the digits, stored one by one to two ping-pong operand slots in tensor
 //     memory (a slot takes digit s once the MMAs of digit s - 2 are done); then the read-back of the
@@ -320,6 +321,7 @@ __global__ void __maxnreg__(kRegs)
     __shared__ uint32_t rpos[32];
     __shared__ __align__(8) uint64_t bar_tma[2];      // tile loaded into buffer b (TMA bytes)
     __shared__ __align__(8) uint64_t bar_written[2];  // tile results written to buffer b (math warps)
+    __shared__ __align__(8) uint64_t bar_drained[2];  // a store from buffer b has read it out (copy warp)
     __shared__ __align__(8) uint64_t bar_full[2];     // operand slot holds the next digit (math warps)
     __shared__ __align__(8) uint64_t bar_mma[2];      // that digit's MMAs are done (commit)
     __shared__ __align__(8) uint64_t bar_acc;         // accumulators read back (math warps)
@@ -384,6 +386,7 @@ __global__ void __maxnreg__(kRegs)
         for (int i = 0; i < 2; ++i) {
             mbar_init(&bar_tma[i], 1);
             mbar_init(&bar_written[i], kMathWarps);
+            mbar_init(&bar_drained[i], 1);
             mbar_init(&bar_full[i], kMathWarps);
             mbar_init(&bar_mma[i], 1);
             s_loads[i] = s_loads_seen[i] = s_commits[i] = s_commits_seen[i] = 0;
@@ -425,20 +428,27 @@ __global__ void __maxnreg__(kRegs)
             for (uint32_t s = lane; s < nseg; s += 32)
                 bulk_load(dst + (size_t)s * seg_amps, psi + (base | seg_off[s]), seg_amps * 16u, &bar_tma[b]);
         };
+        // Tile j is loaded into buffer j % 2 and its results are written into the other buffer (after
+        // the next tile there has been sliced), so that a buffer is reloaded two tiles after its last
+        // store: the load has more than a tile to land.  Buffer 0 is first free once tile 0 is sliced.
         uint32_t ph_w = 0;  // phase parity of bar_written[b] in bit b
         for (uint32_t i = 0; i < my_tiles && i < 2; ++i) issue_load(i);
-        for (uint32_t i = 0; i < my_tiles; ++i) {
-            const uint32_t b = i & 1u;
-            if (!wait_or_abort(&bar_written[b], (ph_w >> b) & 1u, abort_flag, err)) break;
-            ph_w ^= 1u << b;
+        bool go = my_tiles > 2 ? wait_or_abort(&bar_written[0], 0u, abort_flag, err) : true;
+        ph_w = 1u;
+        if (go && my_tiles > 2) issue_load(2);
+        for (uint32_t i = 0; go && i < my_tiles; ++i) {
+            const uint32_t x = (i + 1u) & 1u;  // the buffer holding tile i's results
+            if (!wait_or_abort(&bar_written[x], (ph_w >> x) & 1u, abort_flag, err)) break;
+            ph_w ^= 1u << x;
             const uint64_t base = tile_base(first + i * stride);
-            const double2* src = tiles + (size_t)b * kTileAmps;
+            const double2* src = tiles + (size_t)x * kTileAmps;
             for (uint32_t s = lane; s < nseg; s += 32)
                 bulk_store(psi + (base | seg_off[s]), src + (size_t)s * seg_amps, seg_amps * 16u);
             bulk_commit();
-            bulk_wait_read();  // the buffer is free for the tile two ahead
+            bulk_wait_read();  // the buffer is free for the tile three ahead
             __syncwarp();
-            if (i + 2 < my_tiles) issue_load(i + 2);
+            if (lane == 0) mbar_arrive(&bar_drained[x]);
+            if (i + 3 < my_tiles) issue_load(i + 3);
         }
         bulk_wait_all();
     } else if (warp == kMmaWarp) {
@@ -515,6 +525,8 @@ __global__ void __maxnreg__(kRegs)
         };
         bool ok = my_tiles > 0 && prep_tile<kInF64, NA>(tiles, 0, ph_tma, mrow, rp, y, E, sigma, abort_flag, err,
                                                         bar_tma, counter ? s_loads_seen : nullptr);
+        __syncwarp();
+        if (ok && lane == 0) mbar_arrive(&bar_written[0]);  // buffer 0 sliced: it may take tile 2
         if (ok) {
             put_digit<0, NA>(y, slot0, &bar_full[0], lane);
             put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
@@ -579,7 +591,10 @@ __global__ void __maxnreg__(kRegs)
                 put_digit<0, NA>(y, slot0, &bar_full[0], lane);
                 put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
             }
-            double2* tile = tiles + (size_t)b * kTileAmps;
+            // the results go to the other buffer (its tile, the next, was sliced above); after the last
+            // tile, once the store from that buffer two tiles back has read it out
+            if (!has_next && i >= 2 && !wait_or_abort(&bar_drained[b ^ 1u], ((i >> 1) - 1u) & 1u, abort_flag, err)) break;
+            double2* tile = tiles + (size_t)(b ^ 1u) * kTileAmps;
 #pragma unroll
             for (int k = 0; k < NA; ++k) {
                 const int64_t v0 = (int64_t)acc[2 * k], v1 = (int64_t)acc[2 * k + 1];
@@ -593,7 +608,7 @@ __global__ void __maxnreg__(kRegs)
             }
             fence_proxy_async();  // the results are read by the TMA store
             __syncwarp();
-            if (lane == 0) mbar_arrive(&bar_written[b]);
+            if (lane == 0) mbar_arrive(&bar_written[b ^ 1u]);
         }
         if constexpr (!kOutF64) {
             mag = __reduce_or_sync(0xffffffffu, mag);
