@@ -17,8 +17,8 @@
 // seven balanced base-256 digits (|digit| <= 128), exact in fp16.  The product is the sum over digit
 // pairs (s, t) of A_s B_t^T weighted by 2^(96 - 8 (s + t)); the 34 pairs with s + t <= 7 are issued as
 // tcgen05.mma kind::f16 (M = 128 rows, K = 16) into eight FP32 accumulators in tensor memory, one per
-// level l = s + t (the pairs of one digit s into adjacent levels as one MMA of N = 64 m, m <= 4: 12
-// MMAs per K step instead of 34; an MMA costs about the same for any N up to 256).  Every partial sum is an integer below 2^23 in magnitude (at most 7 products
+// level l = s + t (the pairs of one digit s into adjacent levels as one MMA of N = 64 m, m <= 4: 11
+// MMAs per K step instead of 34; an MMA of N = 64 costs 114 cycles, one of N = 256 181).  Every partial sum is an integer below 2^23 in magnitude (at most 7 products
 // of 64 terms of |digit product| <= 2^14, those with a top digit smaller), so the FP32 accumulation is
 // exact.  Levels >= 8 are dropped (2^-23 of an output unit per level-8 unit: typically 0.01 unit).
 // The accumulators are read back (tcgen05.ld), turned into integers (a magic-number add below 2^22,
@@ -93,7 +93,9 @@ constexpr uint32_t kSlotCol = 448;              // tensor-memory columns of the 
 __host__ __device__ constexpr uint32_t level_col(int l) { return l == 0 ? 384u : 64u * (uint32_t)(l - 1); }
 constexpr uint64_t kBias = 0x80808080808080ull; // 128 in each of the 7 digit bytes
 constexpr uint32_t kMagic = 0x4B400000u;        // bits of 1.5 * 2^23
-constexpr size_t kSmemDyn = 2 * (size_t)kTileAmps * 16 + kWBlockBytes;
+// shared memory: two tile buffers, the block's 7 digit matrices and a copy of digit 0 after digit 6
+// (so that the pairs (0, 5), (0, 6), (0, 0) into levels 5, 6, 0 are one operand)
+constexpr size_t kSmemDyn = 2 * (size_t)kTileAmps * 16 + kWBlockBytes + kWDigitBytes;
 
 // Instruction descriptor of kind::f16: FP32 accumulator, A and B fp16 and K-major, M = 128, N = 64 m
 // (m levels side by side: m digit matrices of a block, stacked 8 KB apart, are one operand of 64 m
@@ -210,6 +212,32 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
 
 // Digit S (0 = most significant) of the thread's 2 NA reals into an operand slot, then one arrival
 // per warp on the slot's "full" barrier.
+// Digits 0 and 1 of the thread's 2 NA reals into the two slots, with one wait for both stores.
+template <int NA>
+__device__ __forceinline__ void put_digits01(const uint64_t (&y)[2 * NA], uint32_t slot_addr, uint64_t* full,
+                                             uint32_t lane) {
+    uint32_t v0[NA], v1[NA];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {
+        v0[i] = digit_pair(y[2 * i], y[2 * i + 1], 6);
+        v1[i] = digit_pair(y[2 * i], y[2 * i + 1], 5);
+    }
+    if constexpr (NA == 16) {
+        tmem_st16(slot_addr, v0);
+        tmem_st16(slot_addr + 32u, v1);
+    } else {
+        tmem_st8(slot_addr, v0);
+        tmem_st8(slot_addr + 32u, v1);
+    }
+    tmem_st_wait();
+    tc_before_sync();
+    __syncwarp();
+    if (lane == 0) {
+        mbar_arrive(&full[0]);
+        mbar_arrive(&full[1]);
+    }
+}
+
 template <int S, int NA>
 __device__ __forceinline__ void put_digit(const uint64_t (&y)[2 * NA], uint32_t tmem_slot_addr, uint64_t* full,
                                           uint32_t lane) {
@@ -377,6 +405,7 @@ __global__ void __maxnreg__(kRegs)
         const uint4* src = reinterpret_cast<const uint4*>(wts + P.w_off);
         uint4* dst = reinterpret_cast<uint4*>(w_sm);
         for (uint32_t i = tid; i < kWBlockBytes / 16; i += kNT) dst[i] = __ldg(src + i);
+        for (uint32_t i = tid; i < kWDigitBytes / 16; i += kNT) dst[kWBlockBytes / 16 + i] = __ldg(src + i);
     }
     if (warp == 0) {
         tmem_alloc(&tmem_base, 512);
@@ -481,10 +510,9 @@ __global__ void __maxnreg__(kRegs)
                 };
                 if (ok && lane == 0) {
                     tc_after_sync();
-                    if (s == 0) {  // levels 1..4, 5..6, then level 0 (its own columns)
+                    if (s == 0) {  // levels 1..4, then 5, 6 and 0 (digit matrices 5, 6 and the copy of 0)
                         issue(1, 4, true);
-                        issue(5, 2, true);
-                        issue(0, 1, true);
+                        issue(5, 3, true);
                     } else {       // levels s .. 7; for digit 1, levels 5..7 once level 0 is read and cleared
                         issue(0, min(4, 8 - s), false);
                     }
@@ -527,10 +555,7 @@ __global__ void __maxnreg__(kRegs)
                                                         bar_tma, counter ? s_loads_seen : nullptr);
         __syncwarp();
         if (ok && lane == 0) mbar_arrive(&bar_written[0]);  // buffer 0 sliced: it may take tile 2
-        if (ok) {
-            put_digit<0, NA>(y, slot0, &bar_full[0], lane);
-            put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
-        }
+        if (ok) put_digits01<NA>(y, slot0, bar_full, lane);
         const uint32_t acc_addr = tmem + lane_addr + 2u * NA * cg;  // this thread's columns at column 0
         for (uint32_t i = 0; ok && i < my_tiles; ++i) {
             const uint32_t b = i & 1u;
@@ -587,10 +612,7 @@ __global__ void __maxnreg__(kRegs)
             if (has_next)
                 ok = prep_tile<kInF64, NA>(tiles, b ^ 1u, ph_tma, mrow, rp, y, E, sigma, abort_flag, err, bar_tma,
                                            counter ? s_loads_seen : nullptr);
-            if (has_next && ok) {
-                put_digit<0, NA>(y, slot0, &bar_full[0], lane);
-                put_digit<1, NA>(y, slot0 + 32u, &bar_full[1], lane);
-            }
+            if (has_next && ok) put_digits01<NA>(y, slot0, bar_full, lane);
             // the results go to the other buffer (its tile, the next, was sliced above); after the last
             // tile, once the store from that buffer two tiles back has read it out
             if (!has_next && i >= 2 && !wait_or_abort(&bar_drained[b ^ 1u], ((i >> 1) - 1u) & 1u, abort_flag, err)) break;
