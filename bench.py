@@ -49,14 +49,16 @@ PROFILE_TRAFFIC = {"fused": os.path.join(ROOT, "profiles", "fused_pass_traffic.j
                    "tensor64": os.path.join(ROOT, "profiles", "tensor64_pass_traffic.json")}
 KERNEL = {"tensor64": "tensor64_pass_kernel", "fused": "fused_df_kernel", "plain": "plain_gate_kernel"}
 ARITHMETIC = {
-    "tensor64": "IEEE f64 storage; dense 5-qubit blocks on tcgen05 with 53-bit operands split into 7 exact fp16 "
-                "digits (28 digit products, FP32 accumulation of integers below 2^23, exact), integer "
-                "reconstruction and one rounding to f64 per block; no FP64 instruction",
+    "tensor64": "IEEE f64 at every call boundary; between the passes of a call 64-bit block floating point "
+                "(int64 components, one exponent per register, the largest renormalised to 2^53..2^54 before "
+                "each pass); dense 5-qubit blocks on tcgen05, each operand split into 7 exact fp16 digits "
+                "(34 digit products, FP32 accumulation of integers below 2^23, exact), one rounding per pass "
+                "to 2^-54 of the largest component; no FP64 instruction",
     "plain": "IEEE f64, one pass per SingleOp in qvnt's operand order, bit-identical to the oracle",
     "fused": "double-float (pairs of FP32 with error-free transforms, 48-bit significand, FP32 exponent range) on "
              "the FP32 pipes, within 1e-12 of the IEEE f64 oracle",
 }
-DTYPE = {"tensor64": "f64", "plain": "f64", "fused": "df64 (2 x f32, 48-bit significand)"}
+DTYPE = {"tensor64": "f64 (int64 block floating point between passes)", "plain": "f64", "fused": "df64 (2 x f32, 48-bit significand)"}
 
 
 def parse():

@@ -108,11 +108,14 @@ typedef struct qvnt_reg qvnt_reg;
  *          (32 x 32 complex) contracted on the tensor cores (TF32 split hi + lo, FP32 accumulation);
  *          norms, probabilities and measurement stay FP64.  Registers of at least 12 qubits; gates
  *          whose targets and controls span more than 5 qubits are rejected (QVNT_ERR_UNSUPPORTED).
- *   TENSOR64 keeps IEEE f64 amplitudes (the PLAIN layout) and fuses runs of gates into dense 5-qubit
- *          blocks contracted on the tensor cores with 53-bit operands split into exact fp16 digit
- *          products (FP32 accumulation of integers below 2^23, no rounding), one f64 rounding per
- *          block; gates spanning more than 5 qubits with their controls, and registers below 12
- *          qubits, run on the PLAIN kernels.  Within 1e-12 of the PLAIN engine. */
+ *   TENSOR64 keeps IEEE f64 amplitudes (the PLAIN layout) between calls and fuses runs of gates into
+ *          dense 5-qubit blocks contracted on the tensor cores: both operands split into exact fp16
+ *          digit products (FP32 accumulation of integers below 2^23, no rounding).  Between the passes
+ *          of one call the state is 64-bit block floating point (int64 components, one exponent per
+ *          register), rounded once per pass to 2^-54 of its largest component; components below about
+ *          2^-54 of the largest are not resolved (IEEE f64 would keep them).  Gates spanning more than
+ *          5 qubits with their controls, and registers below 12 qubits, run on the PLAIN kernels.
+ *          Within 1e-12 of the PLAIN engine. */
 enum qvnt_engine { QVNT_ENGINE_FUSED = 0, QVNT_ENGINE_PLAIN = 1, QVNT_ENGINE_PRECISION = 2, QVNT_ENGINE_TENSOR64 = 3 };
 
 /* ---------------------------------------------------------------------------------------------
