@@ -78,6 +78,9 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-engine", default="fused", choices=["tensor64", "fused"],
+                    help="engine of the serving form's registers (fused: small CTAs share an SM with other "
+                         "requests' tiles; a tensor64 CTA holds a whole SM)")
     ap.add_argument("--cpu-per-class", type=int, default=3, help="gates per stratum in the cpu_baseline sample")
     ap.add_argument("--precision-qubits", type=int, default=32)
     ap.add_argument("--precision-depth", type=int, default=60)
@@ -664,14 +667,14 @@ def main():
                 elif form == "batch":
                     forms["batch"] = bench_batch(ctx, args.batch_count, max(1, min(args.steps, 5)), args.batch_fusion)
                 elif form == "serve":
-                    # the double-float engine with one CTA per tile, so that small requests' tiles
+                    # server registers launch one CTA per tile, so that small requests' tiles
                     # interleave with large requests' passes
-                    forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds, ENGINE_FUSED)
-                    forms["serve"]["engine"] = "fused (double-float)"
+                    se = {"tensor64": ENGINE_TENSOR64, "fused": ENGINE_FUSED}[args.serve_engine]
+                    forms["serve"] = bench_serve(ctx, args.serve_rate, args.serve_seconds, se)
+                    forms["serve"]["engine"] = {"tensor64": "tensor64 (f64)", "fused": "fused (double-float)"}[args.serve_engine]
                     # the same request mix at a rate one GPU sustains (the configured rate is about
                     # two orders of magnitude above its capacity for this mix)
-                    forms["serve"]["at_sustainable_rate"] = bench_serve(ctx, 4.0, min(args.serve_seconds, 20.0),
-                                                                        ENGINE_FUSED)
+                    forms["serve"]["at_sustainable_rate"] = bench_serve(ctx, 4.0, min(args.serve_seconds, 20.0), se)
                     # the plain f64 GPU path serving the same mix (20 s of the same Poisson stream)
                     pl = bench_serve(ctx, args.serve_rate, min(args.serve_seconds, 20.0), ENGINE_PLAIN)
                     forms["serve"]["plain_f64_gpu"] = {

@@ -13,13 +13,17 @@ namespace qvnt {
 constexpr uint32_t kFusedMinK = 6;
 constexpr uint32_t kFusedMaxK = 13;
 
-// Buffers an engine keeps between apply calls (the precision engine's dense-block weights: a device
-// buffer and its pinned host mirror for the upload).
+// Buffers an engine keeps between apply calls (the dense-block weights of the precision and tensor
+// engines: a device buffer and its pinned host mirror for the upload).  They grow to powers of two and
+// never synchronise the device while they grow: the device buffer is stream-ordered (allocated and
+// freed on the register's stream), and an outgrown pinned buffer is kept until the register is freed
+// (freeing pinned memory waits for the whole device, which would stall every other stream of a server).
 struct EngineBuffers {
     void* d_buf = nullptr;
     size_t d_bytes = 0;
     void* h_buf = nullptr;  // pinned host mirror for the upload
     size_t h_bytes = 0;
+    std::vector<void*> retired;      // outgrown pinned mirrors, freed with the register
     cudaEvent_t uploaded = nullptr;  // recorded on the register's stream after the last upload from h_buf
     void release();
     // Buffers of at least `bytes`; h_buf may be written once this returns (the last upload from it is

@@ -1722,6 +1722,8 @@ __global__ void batch_basis_kernel(float4* __restrict__ psi, const uint64_t* __r
 void EngineBuffers::release() {
     if (d_buf) cudaFree(d_buf);
     if (h_buf) cudaFreeHost(h_buf);
+    for (void* p : retired) cudaFreeHost(p);
+    retired.clear();
     if (uploaded) cudaEventDestroy(uploaded);
     d_buf = nullptr;
     h_buf = nullptr;
@@ -1730,15 +1732,24 @@ void EngineBuffers::release() {
 }
 
 int EngineBuffers::acquire(size_t bytes, cudaStream_t stream) {
-    if (d_bytes >= bytes && h_bytes >= bytes) {
-        if (uploaded) QVNT_CUDA_TRY(cudaEventSynchronize(uploaded));
-        return QVNT_OK;
+    if (uploaded) QVNT_CUDA_TRY(cudaEventSynchronize(uploaded));  // the last upload from h_buf is done
+    size_t cap = (size_t)1 << 20;
+    while (cap < bytes) cap <<= 1;
+    if (d_bytes < bytes) {
+        // stream-ordered: the old buffer is freed after the passes queued before this call read it
+        if (d_buf) QVNT_CUDA_TRY(cudaFreeAsync(d_buf, stream));
+        d_buf = nullptr;
+        d_bytes = 0;
+        QVNT_CUDA_TRY(cudaMallocAsync(&d_buf, cap, stream));
+        d_bytes = cap;
     }
-    if (d_buf || h_buf) QVNT_CUDA_TRY(cudaStreamSynchronize(stream));  // passes may still read d_buf
-    release();
-    QVNT_CUDA_TRY(cudaMalloc(&d_buf, bytes));
-    QVNT_CUDA_TRY(cudaMallocHost(&h_buf, bytes));
-    d_bytes = h_bytes = bytes;
+    if (h_bytes < bytes) {
+        if (h_buf) retired.push_back(h_buf);
+        h_buf = nullptr;
+        h_bytes = 0;
+        QVNT_CUDA_TRY(cudaMallocHost(&h_buf, cap));
+        h_bytes = cap;
+    }
     return QVNT_OK;
 }
 
