@@ -8,9 +8,10 @@ from {rxx, ryy, rzz, swap, i_swap, sqrt_i_swap}, 3 Toffolis, then qft over all 3
 Inputs are seeded synthetic circuits (no public suite).  The state (16 GiB) is larger than L2
 (129 MB), so no flush is needed between steps.
 
-The headline engine is TENSOR64: IEEE f64 amplitudes, gates fused into dense 5-qubit blocks and
-contracted on the tensor cores with 53-bit operands split into exact fp16 digit products (no FP64
-instruction, one f64 rounding per block).  Printed as one JSON line (rank 0):
+The headline engine is TENSOR64: IEEE f64 amplitudes at the call boundary, 64-bit block floating
+point between passes, gates fused into dense 5-qubit blocks and contracted on the tensor cores as
+exact fp16 digit products (no FP64 instruction, one rounding per pass to 2^-54 of the largest
+component).  Printed as one JSON line (rank 0):
   value        unfused gate passes per second (qvnt SingleOps), whole job, device-timed
   e2e          the same metric through the plugin call qvnt_apply_host (Applicable::apply): the
                state goes host -> device -> host from pinned memory inside the timed region
