@@ -759,10 +759,10 @@ PassKernel forms_of() {
     return k;
 }
 
-// The layouts in order of preference (measured on a 30-qubit pass of the earlier per-row-exponent
-// form: 17.1 ms against 20.3 ms): 16 math warps of 8 amplitudes with 96 registers (five of the
-// eighteen warps share an SM sub-partition's 16K registers), 8 math warps of 16 amplitudes with 168
-// registers (three of ten); QVNT_T64_LAYOUT=8 or 16 picks one (amplitudes per math thread).
+// The layouts in order of preference (measured on the 30-qubit circuit: 9.45 ms against 10.9 ms per
+// pass): 16 math warps of 8 amplitudes with 96 registers (five of the eighteen warps share an SM
+// sub-partition's 16K registers), 8 math warps of 16 amplitudes with 168 registers (three of ten);
+// QVNT_T64_LAYOUT=8 or 16 picks one (amplitudes per math thread).
 PassKernel pick_kernel() {
     PassKernel out;
     struct Cand {
