@@ -241,3 +241,16 @@ def test_precision_against_high_precision_reference(n):
     e_t64, e_f64 = _hp_error(got, ref), _hp_error(want, ref)
     print("n=%d: tensor64 %.3e, f64 gate by gate %.3e (relative to max |psi|)" % (n, e_t64, e_f64))
     assert e_t64 <= REL_HP and e_t64 <= 2.0 * e_f64
+
+
+def test_nonfinite_block_runs_on_plain_kernels():
+    """A block whose matrix is not finite (a rotation by NaN) is not split into digits: the run of gates
+    it belongs to goes to the plain kernels, so the result equals the PLAIN engine's bit for bit (NaNs
+    in the same places)."""
+    n = 13
+    circ = random_circuit(n, 2, seed=31) * op.rx(float("nan"), 1 << 4) * op.h(0b101)
+    a = run(n, 3, circ).amplitudes()
+    b = run(n, 3, circ, ENGINE_PLAIN).amplitudes()
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    ok = ~np.isnan(a)
+    assert np.array_equal(a[ok], b[ok])
