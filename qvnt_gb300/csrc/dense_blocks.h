@@ -171,7 +171,7 @@ inline std::vector<size_t> block_trial(const std::vector<LGate>& lg, const std::
 
 // Blocks: each is the largest of the candidate blocks seeded by the first kSeeds unplaced gates.
 inline void make_blocks(const std::vector<LGate>& lg, uint32_t L, std::vector<Block>& blocks) {
-    constexpr size_t kSeeds = 48;
+    constexpr size_t kSeeds = 96;
     blocks.clear();
     const size_t n = lg.size();
     std::vector<char> done(n, 0);
