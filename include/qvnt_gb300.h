@@ -332,6 +332,13 @@ int qvnt_precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_nu
  * dense 5-qubit block each) and gates left to single PLAIN passes (no counterpart in the reference). */
 int qvnt_tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* passes,
                             uint64_t* plain_gates);
+/* The dense 5-qubit blocks the TENSOR64 engine would run for a gate list on q_num (>= 5) qubits, in
+ * order (the planner of the tensor and precision engines; no counterpart in the reference).  Every gate
+ * must span at most 5 qubits with its controls (else QVNT_ERR_UNSUPPORTED).  *nblocks = the number of
+ * blocks; when cap >= *nblocks, sups[i] = block i's 5 qubits (a mask) and mats[2048 i ...] its 32 x 32
+ * unitary, row-major, interleaved (re, im), local bit j = the j-th lowest qubit of sups[i]. */
+int qvnt_dense_plan_blocks(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* sups, double* mats,
+                           size_t cap, size_t* nblocks);
 /* Time the fused engine spends in its dominant kernel: CUDA events recorded around every launch of
  * the fused-pass kernel on the register's stream since the last reset (enable != 0 turns
  * recording on and clears the totals).  *ms = summed event time, *launches = number of launches. */

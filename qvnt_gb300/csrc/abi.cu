@@ -900,6 +900,20 @@ int qvnt_tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num
     return tensor64_plan_info(gates, count, (uint32_t)__builtin_ctzll(len), passes, plain_gates);
 }
 
+int qvnt_dense_plan_blocks(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* sups, double* mats,
+                           size_t cap, size_t* nblocks) {
+    if (!gates && count) return set_error(QVNT_ERR_BAD_ARG, "null gate list");
+    if (!nblocks) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
+    if (q_num < 5 || q_num > kMaxQubits) return set_error(QVNT_ERR_BAD_ARG, "q_num %u outside 5..%u", q_num, kMaxQubits);
+    if (cap && (!sups || !mats)) return set_error(QVNT_ERR_BAD_ARG, "null block buffers");
+    const uint64_t len = 1ull << q_num;
+    for (size_t k = 0; k < count; ++k) {
+        int st = validate_gate(gates[k], len);
+        if (st) return set_error(st, "gate %zu: %s", k, qvnt_last_error());
+    }
+    return tensor64_plan_blocks(gates, count, q_num, sups, mats, cap, nblocks);
+}
+
 int qvnt_reg_stats(const qvnt_reg* reg, uint64_t* kernel_launches, uint64_t* passes) {
     CHECK_REG(reg);
     if (kernel_launches) *kernel_launches = reg->launches;

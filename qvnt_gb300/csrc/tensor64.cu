@@ -924,4 +924,22 @@ int tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_
     return QVNT_OK;
 }
 
+int tensor64_plan_blocks(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* sups, double* mats, size_t cap,
+                         size_t* nblocks) {
+    std::vector<dense::LGate> lg;
+    TRY_T(dense::lower_dense(gates, count, lg));
+    std::vector<dense::Block> blocks;
+    dense::make_blocks(lg, L, blocks);
+    *nblocks = blocks.size();
+    if (cap < blocks.size()) return QVNT_OK;
+    for (size_t i = 0; i < blocks.size(); ++i) {
+        sups[i] = blocks[i].sup;
+        for (int e = 0; e < dense::kBD * dense::kBD; ++e) {
+            mats[2048 * i + 2 * e] = blocks[i].u[e].re;
+            mats[2048 * i + 2 * e + 1] = blocks[i].u[e].im;
+        }
+    }
+    return QVNT_OK;
+}
+
 }  // namespace qvnt
