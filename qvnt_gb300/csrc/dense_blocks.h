@@ -169,9 +169,11 @@ inline std::vector<size_t> block_trial(const std::vector<LGate>& lg, const std::
     return members;
 }
 
-// Blocks: each is the largest of the candidate blocks seeded by the first kSeeds unplaced gates.
-inline void make_blocks(const std::vector<LGate>& lg, uint32_t L, std::vector<Block>& blocks) {
-    constexpr size_t kSeeds = 96;
+// Blocks: each is the largest of the candidate blocks seeded by the first `seeds` unplaced gates (the
+// tensor engine takes 96, which plans QFT-heavy circuits into fewer blocks; the precision engine 48,
+// whose passes pair blocks and pair the blocks of the smaller search better).
+inline void make_blocks(const std::vector<LGate>& lg, uint32_t L, std::vector<Block>& blocks, size_t seeds = 48) {
+    const size_t kSeeds = seeds;
     blocks.clear();
     const size_t n = lg.size();
     std::vector<char> done(n, 0);

@@ -735,7 +735,7 @@ int plan_blocks(const qvnt_gate* gates, size_t count, uint32_t L, std::vector<de
                 std::vector<dense::PPlan>& passes) {
     std::vector<dense::LGate> lg;
     TRY_T(dense::lower_dense(gates, count, lg));
-    dense::make_blocks(lg, L, blocks);
+    dense::make_blocks(lg, L, blocks, 96);
     return dense::make_passes(blocks, L, kTQ, kLowQ, 1, passes);
 }
 
@@ -929,7 +929,7 @@ int tensor64_plan_blocks(const qvnt_gate* gates, size_t count, uint32_t L, uint6
     std::vector<dense::LGate> lg;
     TRY_T(dense::lower_dense(gates, count, lg));
     std::vector<dense::Block> blocks;
-    dense::make_blocks(lg, L, blocks);
+    dense::make_blocks(lg, L, blocks, 96);
     *nblocks = blocks.size();
     if (cap < blocks.size()) return QVNT_OK;
     for (size_t i = 0; i < blocks.size(); ++i) {
