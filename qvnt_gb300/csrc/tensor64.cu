@@ -17,14 +17,15 @@
 // seven balanced base-256 digits (|digit| <= 128), exact in fp16.  The product is the sum over digit
 // pairs (s, t) of A_s B_t^T weighted by 2^(96 - 8 (s + t)); the 34 pairs with s + t <= 7 are issued as
 // tcgen05.mma kind::f16 (M = 128 rows, K = 16) into eight FP32 accumulators in tensor memory, one per
-// level l = s + t (the pairs of one digit s into adjacent levels as one MMA of N = 64 m, m <= 4: 11
-// MMAs per K step instead of 34; an MMA of N = 64 costs 114 cycles, one of N = 256 181).  Every partial sum is an integer below 2^23 in magnitude (at most 7 products
-// of 64 terms of |digit product| <= 2^14, those with a top digit smaller), so the FP32 accumulation is
-// exact.  Levels >= 8 are dropped (2^-23 of an output unit per level-8 unit: typically 0.01 unit).
-// The accumulators are read back (tcgen05.ld), turned into integers (a magic-number add below 2^22,
-// an exact float-to-int conversion above), and combined into the output X' = sum_l L_l 2^(41 - 8 l)
-// with one rounding (of the levels 6 and 7 part, to within 1/2 + 2^-9 of a unit); no FP64
-// instruction is issued.
+// level l = s + t: the pairs of one digit s into adjacent levels are one MMA of N = 64 m, m <= 4, so a
+// K step takes 11 MMAs instead of 34 (an MMA of N = 64 costs 114 cycles, one of N = 256 181).  Every
+// partial sum is an integer below 2^23 in magnitude (at most 7 products of 64 terms of |digit product|
+// <= 2^14, those with a top digit smaller), so the FP32 accumulation is exact.  Levels >= 8 are
+// dropped (2^-23 of an output unit per level-8 unit: typically 0.01 unit).  The accumulators are read
+// back (tcgen05.ld): levels 0-3 as integers by a magic-number add (below 2^22), levels 4-5 by an exact
+// float-to-int conversion, and L6 2^-7 + L7 2^-15 summed in FP32; they combine into the output
+// X' = sum_l L_l 2^(41 - 8 l) with one rounding (of the levels 6 and 7 part, to within 1/2 + 2^-9 of
+// a unit).  No FP64 instruction is issued.
 //
 // Kernel (one pass = one block): persistent CTAs, one per SM (tensor memory: all 512 columns), of
 // 18 warps (10 in the 16-amplitude layout) in three roles synchronised by mbarriers only.  Per tile of
