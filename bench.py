@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--mma-costs", action="store_true",
+                    help="print the tensor-core instruction costs that bound the TENSOR64 pass, then exit")
     ap.add_argument("--serve-engine", default="fused", choices=["tensor64", "fused"],
                     help="engine of the serving form's registers (fused: small CTAs share an SM with other "
                          "requests' tiles; a tensor64 CTA holds a whole SM)")
@@ -510,11 +512,29 @@ def bench_df64(ctx, circ_arr, ngates, n, steps):
             "kernel_gbs": algorithmic_pass_bytes(n) / (avg / 1e3) / 1e9 if avg else None}
 
 
+def mma_costs(device):
+    """The tensor-core instruction costs that bound the TENSOR64 pass (SM cycles, all SMs issuing):
+    one tcgen05.mma.kind::f16 (M = 128, K = 16) of N = 64 and of N = 256, and a pass tile's 44 MMAs."""
+    import ctypes
+    from qvnt_gb300 import Context
+    from qvnt_gb300._abi import check, lib
+    ctx = Context(device)
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    check(lib().qvnt_tensor64_mma_costs(ctx.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+    print(json.dumps({"measurement": "tcgen05.mma.kind::f16 cost, M = 128, K = 16, A from tensor memory",
+                      "cycles_per_mma_n64": a.value, "cycles_per_mma_n256": b.value,
+                      "cycles_per_pass_tile_44_mmas": c.value}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.mma_costs:
+        mma_costs(local)
         return
     import numpy as np
     import torch

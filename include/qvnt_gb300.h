@@ -339,6 +339,11 @@ int qvnt_tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num
  * unitary, row-major, interleaved (re, im), local bit j = the j-th lowest qubit of sups[i]. */
 int qvnt_dense_plan_blocks(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* sups, double* mats,
                            size_t cap, size_t* nblocks);
+/* The cost, in SM cycles, of the TENSOR64 pass's tensor-core instructions measured in isolation on
+ * every SM of the context's device: one tcgen05.mma.kind::f16 (M = 128, K = 16) of N = 64 and of
+ * N = 256, and the 44 MMAs of one pass tile (the pass's mix of N = 64 .. 256).  A measurement, not
+ * part of the path. */
+int qvnt_tensor64_mma_costs(qvnt_ctx* ctx, double* n64_cycles, double* n256_cycles, double* tile_cycles);
 /* Time the fused engine spends in its dominant kernel: CUDA events recorded around every launch of
  * the fused-pass kernel on the register's stream since the last reset (enable != 0 turns
  * recording on and clears the totals).  *ms = summed event time, *launches = number of launches. */

@@ -108,6 +108,7 @@ _PROTOS = {
     "qvnt_reg_linear_composition": (c_int, [c_void, c_void, P(c_double)]),
     "qvnt_precision_plan_info": (c_int, [P(QvntGate), c_size, c_u32, P(c_u64), P(c_u64)]),
     "qvnt_dense_plan_blocks": (c_int, [P(QvntGate), c_size, c_u32, P(c_u64), P(c_double), c_size, P(c_size)]),
+    "qvnt_tensor64_mma_costs": (c_int, [c_void, P(c_double), P(c_double), P(c_double)]),
     "qvnt_tensor64_plan_info": (c_int, [P(QvntGate), c_size, c_u32, P(c_u64), P(c_u64)]),
     "qvnt_ctx_set_engine": (c_int, [c_void, c_int]),
     "qvnt_reg_destroy": (c_int, [c_void]),

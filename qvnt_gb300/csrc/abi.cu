@@ -900,6 +900,12 @@ int qvnt_tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t q_num
     return tensor64_plan_info(gates, count, (uint32_t)__builtin_ctzll(len), passes, plain_gates);
 }
 
+int qvnt_tensor64_mma_costs(qvnt_ctx* ctx, double* n64_cycles, double* n256_cycles, double* tile_cycles) {
+    CHECK_CTX(ctx);
+    if (!n64_cycles || !n256_cycles || !tile_cycles) return set_error(QVNT_ERR_BAD_ARG, "null output pointer");
+    return tensor64_mma_costs(ctx->device, ctx->geo.sms, n64_cycles, n256_cycles, tile_cycles);
+}
+
 int qvnt_dense_plan_blocks(const qvnt_gate* gates, size_t count, uint32_t q_num, uint64_t* sups, double* mats,
                            size_t cap, size_t* nblocks) {
     if (!gates && count) return set_error(QVNT_ERR_BAD_ARG, "null gate list");

@@ -87,6 +87,7 @@ int apply_precision(qvnt_reg* r, const qvnt_gate* gates, size_t count);
 int precision_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* blocks);
 int apply_tensor64(qvnt_reg* r, const qvnt_gate* gates, size_t count);
 int tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* passes, uint64_t* plain_gates);
+int tensor64_mma_costs(int device, int sms, double* n64, double* n256, double* tile);
 int tensor64_plan_blocks(const qvnt_gate* gates, size_t count, uint32_t L, uint64_t* sups, double* mats, size_t cap,
                          size_t* nblocks);
 int launch_inv(const double* d_abs, double* d_inv, int* d_status, cudaStream_t stream);

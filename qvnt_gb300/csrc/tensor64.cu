@@ -18,7 +18,7 @@
 // pairs (s, t) of A_s B_t^T weighted by 2^(96 - 8 (s + t)); the 34 pairs with s + t <= 7 are issued as
 // tcgen05.mma kind::f16 (M = 128 rows, K = 16) into eight FP32 accumulators in tensor memory, one per
 // level l = s + t: the pairs of one digit s into adjacent levels are one MMA of N = 64 m, m <= 4, so a
-// K step takes 11 MMAs instead of 34 (an MMA of N = 64 costs 114 cycles, one of N = 256 181).  Every
+// K step takes 11 MMAs instead of 34 (an MMA of N = 64 costs 97 cycles, one of N = 256 128).  Every
 // partial sum is an integer below 2^23 in magnitude (at most 7 products of 64 terms of |digit product|
 // <= 2^14, those with a top digit smaller), so the FP32 accumulation is exact.  Levels >= 8 are
 // dropped (2^-23 of an output unit per level-8 unit: typically 0.01 unit).  The accumulators are read
@@ -654,6 +654,63 @@ __global__ void __maxnreg__(kRegs)
     if (warp == 0) tmem_dealloc(tmem_base, 512);
 }
 
+// The cost of the pass's tensor-core instructions, measured in isolation: one thread per CTA issues
+// `reps` rounds of 44 tcgen05.mma kind::f16 (M = 128, K = 16; A from tensor memory, B from shared
+// memory) and waits for their commit; clock64 around it.  mode 0: a tile of the pass (11 MMAs of
+// N = 64 m per K step, the pass's mix); 1: N = 64 only; 2: N = 256 only.  Operand values do not
+// matter (shared memory holds fp16 ones, tensor memory is not initialised).
+__global__ void tensor64_mma_cost_kernel(int mode, int reps, unsigned long long* out, int* err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint32_t tmem_base;
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t i = threadIdx.x; i < (kWBlockBytes + kWDigitBytes) / 4; i += blockDim.x)
+        reinterpret_cast<uint32_t*>(smem)[i] = 0x3C003C00u;
+    if (warp == 0) {
+        tmem_alloc(&tmem_base, 512);
+        tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    fence_proxy_async();
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = tmem_base, w = smem_addr(smem);
+    const unsigned long long t0 = clock64();
+    if (warp == 0 && lane == 0) {
+        for (int it = 0; it < reps; ++it)
+            for (int s = 0; s < kDigits; ++s) {
+                const uint32_t a_tm = tmem + kSlotCol + 32u * (uint32_t)(s & 1);
+                for (uint32_t ks = 0; ks < 4; ++ks) {
+                    const uint64_t bd = smem_desc(w + 256u * ks, 128u, 1024u);
+                    if (mode == 0) {  // the m of each of digit s's MMAs: 4 then 3 (s = 0, 1), 4 then 8 - s - 4, or 8 - s
+                        const int first = s == 0 ? 4 : min(4, 8 - s);
+                        const int second = s == 0 ? 3 : 8 - s - first;
+                        mma_f16_ta(tmem, a_tm + 8u * ks, bd, idesc16((uint32_t)first), 1u);
+                        if (second > 0) mma_f16_ta(tmem + 256u, a_tm + 8u * ks, bd, idesc16((uint32_t)second), 1u);
+                    } else {
+                        // 44 per tile: 6 or 7 per digit and K step
+                        const int n = s < 4 ? 2 : 1;
+                        for (int c = 0; c < n; ++c)
+                            mma_f16_ta(tmem + 128u * (uint32_t)c, a_tm + 8u * ks, bd, idesc16(mode == 1 ? 1u : 4u), 1u);
+                    }
+                }
+            }
+        mma_commit(&bar);
+    }
+    __syncwarp();
+    if (warp == 0 && !mbar_wait(&bar, 0u, 1u << 26)) atomicExch(err, 1);
+    const unsigned long long t1 = clock64();
+    if (threadIdx.x == 0) out[blockIdx.x] = t1 - t0;
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (warp == 0) tmem_dealloc(tmem_base, 512);
+}
+
 // The largest biased f64 exponent of the register's components, into slot 0 of its scale ring (the
 // ring cleared before).
 __global__ void tensor64_maxexp_kernel(const double2* __restrict__ psi, uint64_t len, ScaleSlot* slots) {
@@ -922,6 +979,47 @@ int tensor64_plan_info(const qvnt_gate* gates, size_t count, uint32_t L, uint64_
     }
     if (passes) *passes = np;
     if (plain_gates) *plain_gates = pg;
+    return QVNT_OK;
+}
+
+int tensor64_mma_costs(int device, int sms, double* n64, double* n256, double* tile) {
+    const size_t smem = kWBlockBytes + kWDigitBytes;
+    QVNT_CUDA_TRY(cudaSetDevice(device));
+    QVNT_CUDA_TRY(cudaFuncSetAttribute((const void*)tensor64_mma_cost_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    unsigned long long* d_out = nullptr;
+    int* d_err = nullptr;
+    QVNT_CUDA_TRY(cudaMalloc(&d_out, sizeof(unsigned long long) * (size_t)sms));
+    QVNT_CUDA_TRY(cudaMalloc(&d_err, sizeof(int)));
+    QVNT_CUDA_TRY(cudaMemset(d_err, 0, sizeof(int)));
+    std::vector<unsigned long long> h((size_t)sms);
+    double res[3] = {0, 0, 0};
+    const int reps = 200;
+    int st = QVNT_OK;
+    for (int mode = 0; mode < 3 && !st; ++mode) {
+        for (int rep = 0; rep < 2; ++rep) tensor64_mma_cost_kernel<<<sms, 128, smem>>>(mode, reps, d_out, d_err);
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaMemcpy(h.data(), d_out, sizeof(unsigned long long) * (size_t)sms, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            st = set_cuda_error(e, "mma cost kernel");
+            break;
+        }
+        double avg = 0;
+        for (unsigned long long v : h) avg += (double)v;
+        avg /= (double)sms;
+        res[mode] = mode == 0 ? avg / reps : avg / reps / 44.0;  // per tile, or per MMA
+    }
+    int h_err = 0;
+    if (!st) {
+        cudaMemcpy(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (h_err) st = set_error(QVNT_ERR_TIMEOUT, "mma cost kernel: commit wait ran out");
+    }
+    cudaFree(d_out);
+    cudaFree(d_err);
+    if (st) return st;
+    *tile = res[0];
+    *n64 = res[1];
+    *n256 = res[2];
     return QVNT_OK;
 }
 
